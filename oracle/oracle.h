@@ -1,0 +1,48 @@
+/*
+ * oracle.h -- CPU restatement of the reference's FP64 SpMV path.
+ * TEST INFRASTRUCTURE ONLY (see oracle.c); never part of the product.
+ */
+#ifndef SBLAS_ORACLE_H
+#define SBLAS_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void oracle_csr_spmv(int m, int n, int nnz, const double *alpha,
+                     const double *val, const int *rowptr, const int *col,
+                     const double *x, const double *beta, double *y);
+void oracle_csr_spmv_omp(int m, int n, int nnz, const double *alpha,
+                         const double *val, const int *rowptr, const int *col,
+                         const double *x, const double *beta, double *y,
+                         int nthreads);
+void oracle_coo_spmv(int m, int n, int nnz, const double *alpha,
+                     const double *val, const int *rowidx, const int *colidx,
+                     const double *x, const double *beta, double *y);
+void oracle_csc_spmv(int m, int n, int nnz, const double *alpha,
+                     const double *val, const int *colptr, const int *rowidx,
+                     const double *x, const double *beta, double *y);
+void oracle_csr_spmv_dot2(int m, int n, int nnz, const double *alpha,
+                          const double *val, const int *rowptr, const int *col,
+                          const double *x, const double *beta, double *y);
+
+int oracle_get_row_from_index(int n, const int *a, int idx);
+int oracle_find_first_in_sorted(const int *a, int n, int key);
+int oracle_find_last_in_sorted(const int *a, int n, int key);
+
+int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
+                              const double *val, const int *rowptr, const int *col,
+                              const double *x, const double *beta, double *y,
+                              int nparts);
+
+long long oracle_gen_g(int n, int *rowidx, int *colidx, double *val);
+
+void oracle_coo2csr(int m, int n, int nnz, const double *cooval, const int *coorow,
+                    const int *coocol, double *csrval, int *csrrowptr, int *csrcol);
+void oracle_coo2csc(int m, int n, int nnz, const double *cooval, const int *coorow,
+                    const int *coocol, double *cscval, int *csccolptr, int *cscrow);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
