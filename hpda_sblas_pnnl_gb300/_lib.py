@@ -1,0 +1,141 @@
+"""ctypes binding of libsblas_gb300.so (the C ABI in include/*.h).
+
+The library is the product: there is no Python or CPU fallback.  If the
+shared object is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import build as _build
+
+_LIB: C.CDLL | None = None
+
+
+class SpmvRet(C.Structure):
+    """include/spmv_kernel.h:16-57 (spmv_ret): per-phase seconds of one call."""
+
+    _fields_ = [
+        ("numa_part_time", C.c_double),
+        ("part_time", C.c_double),
+        ("comp_time", C.c_double),
+        ("comm_time", C.c_double),
+        ("merg_time", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+    def failed(self) -> bool:
+        return self.comp_time < 0
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+# name -> (restype, argtypes); every symbol declared in include/*.h
+SIGNATURES: dict[str, tuple] = {
+    # include/sblas_gb300.h
+    "sblas_last_error": (C.c_char_p, []),
+    "sblas_last_status": (C.c_int, []),
+    "sblas_version": (C.c_char_p, []),
+    "sblas_set_compat_mode": (None, [C.c_int]),
+    "sblas_get_compat_mode": (C.c_int, []),
+    "sblas_tile_workspace_bytes": (C.c_size_t, [C.c_longlong, C.c_int]),
+    "sblas_tile_sigma_count": (C.c_int, []),
+    "sblas_tile_sigma_at": (C.c_int, [C.c_int]),
+    "sblas_default_sigma": (C.c_int, [C.c_int, C.c_longlong]),
+    "sblas_csr5_sigma": (C.c_int, [C.c_int, C.c_longlong]),
+    "sblas_dcsrmv": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, C.c_int,
+                               _vp, _vp, _vp, C.c_double, _vp, C.c_int, _vp, C.c_size_t, _vp]),
+    "sblas_dcoomv": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, _vp, _vp, _vp,
+                               C.c_double, _vp, _vp, C.c_int, _vp, C.c_size_t, _vp]),
+    "sblas_csc_to_csr_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_longlong]),
+    "sblas_csc_to_csr": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp,
+                                   _vp, C.c_size_t, _vp]),
+    "sblas_coo_rows_to_rowptr": (C.c_int, [C.c_int, C.c_longlong, _vp, _vp, _vp]),
+    # include/spmv_kernel.h (reference signatures)
+    "csr5_kernel": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _vp, _vp, _vp, _dp, _vp, _vp]),
+    "spMV_mgpu_baseline": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,
+                                     _dp, C.c_int]),
+    "spMV_mgpu_baseline_csc": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,
+                                         _dp, C.c_int]),
+    "spMV_mgpu_baseline_coo": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,
+                                         _dp, C.c_int]),
+    "spMV_mgpu_v1": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp,
+                               C.c_int, C.c_int]),
+    "spMV_mgpu_v1_numa": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp,
+                                    C.c_int, C.c_int, _ip, C.c_int, C.c_int]),
+    "spMV_mgpu_v1_numa_csc": (SpmvRet, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _ip, _ip, _dp,
+                                        _dp, _dp, C.c_int, C.c_int, _ip, C.c_int, C.c_int]),
+    "spMV_mgpu_v1_numa_coo": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,
+                                        _dp, C.c_int, C.c_int, _ip, C.c_int, C.c_int]),
+    "spMV_mgpu_v2": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp,
+                               C.c_int, C.c_int, C.c_int, C.c_int]),
+    "spMspV_mgpu_v1": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp,
+                                 C.c_int, C.c_int]),
+    "spMspV_mgpu_v2": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp,
+                                 C.c_int, C.c_int, C.c_int, C.c_int]),
+    "get_row_from_index": (C.c_int, [C.c_int, _ip, C.c_int]),
+    "get_time": (C.c_double, []),
+    "get_gpu_availble_mem": (C.c_double, [C.c_int]),
+    "coo2csr": (None, [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip, _dp, _ip, _ip]),
+    "coo2csc": (None, [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip, _dp, _ip, _ip]),
+    "sortCOORow": (None, [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip]),
+    "sortCOOCol": (None, [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip]),
+    "coo2csrGPU": (None, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "findFirstInSorted": (C.c_int, [_ip, C.c_int, C.c_int]),
+    "findLastInSorted": (C.c_int, [_ip, C.c_int, C.c_int]),
+    "report_mem_usage": (None, [C.c_int]),
+    "report_all_mem_usage": (None, []),
+    "print_vec_double": (None, [_dp, C.c_int, C.c_char_p]),
+    "print_vec_int": (None, [_ip, C.c_int, C.c_char_p]),
+    "print_vec_gpu_double": (None, [_dp, C.c_int, C.c_char_p]),
+    "print_vec_gpu_int": (None, [_ip, C.c_int, C.c_char_p]),
+}
+
+
+class SblasError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"sblas status {status}: {msg}")
+        self.status = status
+
+
+def lib_path() -> Path:
+    env = os.environ.get("SBLAS_GB300_LIB")
+    return Path(env) if env else _build.lib_path()
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Loads libsblas_gb300.so; raises if it is absent (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = lib_path()
+    if not p.exists():
+        if build_if_missing:
+            p = _build.build()
+        else:
+            raise RuntimeError(
+                f"{p} is missing: build it with `python -m hpda_sblas_pnnl_gb300.build` "
+                "(this package has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        lib = load()
+        raise SblasError(rc, lib.sblas_last_error().decode())
+
+
+def last_error() -> str:
+    return load().sblas_last_error().decode()

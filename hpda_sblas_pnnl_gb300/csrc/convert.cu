@@ -1,0 +1,207 @@
+// Format conversion on the device (setup work, not the SpMV hot path).
+//
+// The reference converts on the GPU with cuSPARSE: coo2csrGPU =
+// cusparseXcoo2csr (src/spmv_helper.cu:478-490) after a stable row sort
+// (sortCOORowGPU, :427-443); coo2csc = a stable column sort then the same
+// compression with rows and columns swapped (:575-642).  Here:
+//   * row-sorted COO -> CSR row pointer: atomic-free boundary detection (each
+//     nonzero whose row differs from its left neighbour writes the row
+//     pointer entries of the rows in between);
+//   * CSC -> CSR: a stable radix sort of (row, CSC position) pairs (CUB,
+//     part of the CUDA toolkit), then a gather of column and value; stability
+//     keeps columns ascending inside each row, as cuSPARSE's stable coosort.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "sblas_internal.h"
+
+namespace sblas {
+namespace {
+
+__global__ void coo_rowptr_kernel(int m, long long nnz, const int *__restrict__ row,
+                                  int *__restrict__ rowptr, int *__restrict__ bad)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k <= nnz; k += stride) {
+        const int prev = (k == 0) ? -1 : __ldg(row + k - 1);
+        const int cur = (k == nnz) ? m : __ldg(row + k);
+        if (k < nnz && (cur < 0 || cur >= m)) {
+            if (bad) atomicExch(bad, 1);
+            continue;
+        }
+        if (cur < prev) {
+            if (bad) atomicExch(bad, 1);
+            continue;
+        }
+        // rows prev+1 .. cur start at k (row `cur` itself starts at k too)
+        for (int r = prev + 1; r <= cur && r <= m; ++r) rowptr[r] = (int)k;
+    }
+}
+
+__global__ void zero_rowptr_kernel(int m, int *rowptr)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= m; i += gridDim.x * blockDim.x)
+        rowptr[i] = 0;
+}
+
+__global__ void iota_kernel(long long nnz, int *v)
+{
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+         k += (long long)gridDim.x * blockDim.x)
+        v[k] = (int)k;
+}
+
+// CSC position k -> its column (largest j with colptr[j] <= k, skipping
+// empty columns), then gather column and value into CSR order.
+__global__ void csc_gather_kernel(int n, long long nnz, const int *__restrict__ colptr,
+                                  const int *__restrict__ perm, const double *__restrict__ cval,
+                                  int *__restrict__ ocol, double *__restrict__ oval)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int k = __ldg(perm + p);
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(colptr + mid) <= k) lo = mid; else hi = mid - 1;
+        }
+        ocol[p] = lo;
+        oval[p] = __ldg(cval + k);
+    }
+}
+
+int grid_for(long long items, int threads)
+{
+    const long long want = (items + threads - 1) / threads;
+    const long long cap = 8LL * device_num_sms();
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+int end_bit_for(int m)
+{
+    int b = 1;
+    while (b < 31 && (1LL << b) < (long long)m) ++b;
+    return b;
+}
+
+size_t al256(size_t v) { return (v + 255) & ~size_t(255); }
+
+}  // namespace
+
+int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
+                              cudaStream_t stream)
+{
+    if (m < 0 || nnz < 0) {
+        set_error(SBLAS_ERR_ARG, "negative size");
+        return SBLAS_ERR_ARG;
+    }
+    if (nnz == 0) {
+        zero_rowptr_kernel<<<grid_for((long long)m + 1, 256), 256, 0, stream>>>(m, rowptr);
+    } else {
+        coo_rowptr_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(m, nnz, coo_row, rowptr,
+                                                                    nullptr);
+    }
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
+size_t csc_to_csr_workspace_bytes(int m, int n, long long nnz)
+{
+    (void)n;
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(m));
+    return al256(cub_bytes) + 3 * al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+}
+
+int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val, const int *csc_colptr,
+                      const int *csc_row, double *csr_val, int *csr_rowptr, int *csr_col,
+                      void *work, size_t work_bytes, cudaStream_t stream)
+{
+    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL) {
+        set_error(SBLAS_ERR_ARG, "bad sizes m=%d n=%d nnz=%lld", m, n, nnz);
+        return SBLAS_ERR_ARG;
+    }
+    if (nnz == 0) return launch_coo_rows_to_rowptr(m, 0, nullptr, csr_rowptr, stream);
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(m));
+    const size_t need = al256(cub_bytes) + 3 * al256(sizeof(int) * (size_t)nnz);
+    if (work == nullptr || work_bytes < need) {
+        set_error(SBLAS_ERR_ARG, "csc_to_csr workspace too small (%zu < %zu)", work_bytes, need);
+        return SBLAS_ERR_ARG;
+    }
+    unsigned char *w = static_cast<unsigned char *>(work);
+    void *cub_tmp = w;
+    int *perm_in = reinterpret_cast<int *>(w + al256(cub_bytes));
+    int *perm_out = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * nnz));
+    int *rows_sorted =
+        reinterpret_cast<int *>(w + al256(cub_bytes) + 2 * al256(sizeof(int) * nnz));
+    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, perm_in);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(cub_tmp, cub_bytes, csc_row,
+                                                              rows_sorted, perm_in, perm_out,
+                                                              (int)nnz, 0, end_bit_for(m),
+                                                              stream)));
+    csc_gather_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(n, nnz, csc_colptr, perm_out,
+                                                              csc_val, csr_col, csr_val);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return launch_coo_rows_to_rowptr(m, nnz, rows_sorted, csr_rowptr, stream);
+}
+
+size_t sort_perm_workspace_bytes(int key_bound, long long nnz)
+{
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(key_bound));
+    return al256(cub_bytes) + al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+}
+
+int launch_sort_perm(int key_bound, long long nnz, const int *keys, int *keys_sorted, int *perm,
+                     void *work, size_t work_bytes, cudaStream_t stream)
+{
+    if (nnz <= 0) return SBLAS_OK;
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(key_bound));
+    if (work_bytes < al256(cub_bytes) + al256(sizeof(int) * (size_t)nnz)) {
+        set_error(SBLAS_ERR_ARG, "sort workspace too small");
+        return SBLAS_ERR_ARG;
+    }
+    unsigned char *w = static_cast<unsigned char *>(work);
+    int *iota = reinterpret_cast<int *>(w + al256(cub_bytes));
+    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, iota);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(w, cub_bytes, keys, keys_sorted, iota,
+                                                              perm, (int)nnz, 0,
+                                                              end_bit_for(key_bound), stream)));
+    return SBLAS_OK;
+}
+
+namespace {
+__global__ void gather_kernel(long long nnz, const int *__restrict__ perm,
+                              const int *__restrict__ in_i, int *__restrict__ out_i,
+                              const double *__restrict__ in_d, double *__restrict__ out_d)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int k = __ldg(perm + p);
+        if (out_i) out_i[p] = __ldg(in_i + k);
+        if (out_d) out_d[p] = __ldg(in_d + k);
+    }
+}
+}  // namespace
+
+int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
+                  const double *in_d, double *out_d, cudaStream_t stream)
+{
+    if (nnz <= 0) return SBLAS_OK;
+    gather_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, perm, in_i, out_i, in_d, out_d);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
+}  // namespace sblas

@@ -1,0 +1,102 @@
+// Internal declarations shared by the CUDA translation units of
+// libsblas_gb300.so.  Nothing here is part of the public C ABI
+// (include/sblas_gb300.h and include/spmv_kernel.h are).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/sblas_gb300.h"
+
+namespace sblas {
+
+// ---- error state: thread-local status readable through sblas_last_error ----
+void set_error(int code, const char *fmt, ...);
+void clear_error();
+int last_status();
+
+#define SBLAS_CUDA_TRY(expr)                                                          \
+    do {                                                                              \
+        cudaError_t sblas_e_ = (expr);                                                \
+        if (sblas_e_ != cudaSuccess) {                                                \
+            ::sblas::set_error(SBLAS_ERR_CUDA, "%s failed: %s (%s:%d)", #expr,      \
+                               cudaGetErrorString(sblas_e_), __FILE__, __LINE__);    \
+            return SBLAS_ERR_CUDA;                                                    \
+        }                                                                             \
+    } while (0)
+
+// ---- nnz-tile engine (the load-balanced CSR kernel) ----------------------
+// A tile is TILE_THREADS * sigma consecutive nonzeros.  Workspace per call:
+//   row_part[ntiles + 1]  first owned row of every tile (int32)
+//   carry[ntiles]         FP64 partial of the row that continues past the tile
+//   status[1]             device error flag (bounded waits)
+struct TileShape {
+    int threads;   // threads per CTA
+    int sigma;     // nonzeros per thread
+    long long tile() const { return (long long)threads * sigma; }
+};
+
+// Shapes compiled into the library (sigma odd: conflict-free shared reads).
+int tile_shape_count();
+TileShape tile_shape_at(int i);
+int tile_shape_index(int sigma);   // -1 if not compiled
+
+size_t tile_workspace_bytes(long long nnz, int sigma);
+
+// Value storage of the matrix:  0 = FP64, 1 = FP32 (accumulated in FP64
+// through a double-float product and run sum), 2 = pattern (no value array).
+enum ValueKind { VAL_F64 = 0, VAL_F32 = 1, VAL_PATTERN = 2 };
+
+// Launches partition + tile kernel + carry fix-up on `stream`.
+// `work` must hold tile_workspace_bytes(nnz, sigma) bytes, 256-byte aligned.
+int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
+                     int val_kind, const int *rowptr, const int *col, const double *x,
+                     double beta, double *y, int sigma, void *work, cudaStream_t stream);
+
+// Row-split kernel (one sub-warp per row; kernel version 1).
+int launch_rowsplit_spmv(int m, int n, long long nnz, double alpha, const double *val,
+                         const int *rowptr, const int *col, const double *x, double beta,
+                         double *y, cudaStream_t stream);
+
+// y[i] = beta * y[i] (beta == 0 writes exact zeros), for m == 0 / nnz == 0.
+int launch_scale_y(int m, double beta, double *y, cudaStream_t stream);
+
+// ---- format conversion (setup kernels) ------------------------------------
+// Row-sorted COO row indices -> CSR row pointer (atomic-free boundary scan).
+int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
+                              cudaStream_t stream);
+// CSC -> CSR transpose (stable: columns ascending inside each row).
+size_t csc_to_csr_workspace_bytes(int m, int n, long long nnz);
+int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
+                      const int *csc_colptr, const int *csc_row, double *csr_val,
+                      int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,
+                      cudaStream_t stream);
+
+// Stable sort of int keys in [0, key_bound) carrying their positions:
+// keys_sorted[p] = keys[perm[p]].  Workspace: sort_perm_workspace_bytes.
+size_t sort_perm_workspace_bytes(int key_bound, long long nnz);
+int launch_sort_perm(int key_bound, long long nnz, const int *keys, int *keys_sorted, int *perm,
+                     void *work, size_t work_bytes, cudaStream_t stream);
+// out_i[p] = in_i[perm[p]], out_d[p] = in_d[perm[p]] (either output may be null).
+int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
+                  const double *in_d, double *out_d, cudaStream_t stream);
+
+// ---- per-device resources used by the host (drop-in) entry points --------
+struct DeviceContext {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+};
+// Returns the context of the current device (created on first use).
+DeviceContext *device_context();
+
+// Grow-only device scratch buffers owned by the context (slot 0..15).
+void *device_scratch(int slot, size_t bytes);
+
+int default_sigma_for(int m, long long nnz);
+int csr5_sigma_for(int m, long long nnz);
+int device_num_sms();
+
+}  // namespace sblas

@@ -1,0 +1,121 @@
+/*
+ * sblas_gb300.h -- device-pointer C ABI of libsblas_gb300.so.
+ *
+ * The drop-in entry points with the reference's signatures are declared in
+ * spmv_kernel.h (host pointers, synchronous).  This header is the layer
+ * under them: device pointers, a caller-supplied CUDA stream, asynchronous
+ * and stream-ordered, no allocation inside a call unless stated.  It is what
+ * the Python package (ctypes), CUDA-graph capture and batching use.
+ *
+ * Numerics: y = alpha * A * x + beta * y with A in CSR (int32 indices),
+ * FP64 accumulation.  beta == 0 never reads y (NaNs in y are overwritten).
+ * All functions return SBLAS_OK (0) or a negative status; the message of
+ * the last failure on the calling thread is sblas_last_error().
+ */
+#ifndef SBLAS_GB300_H
+#define SBLAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SBLAS_API __attribute__((visibility("default")))
+#else
+#define SBLAS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SBLAS_OK 0
+#define SBLAS_ERR_ARG (-1)            /* invalid size, pointer or option */
+#define SBLAS_ERR_NGPU (-2)           /* ngpu != 1: one GPU per process */
+#define SBLAS_ERR_CUDA (-3)           /* a CUDA runtime call failed */
+#define SBLAS_ERR_ALLOC (-4)          /* device allocation failed */
+#define SBLAS_ERR_ALIGN (-5)          /* device array not 16-byte aligned */
+#define SBLAS_ERR_KERNEL (-6)         /* a kernel reported a device-side error */
+#define SBLAS_ERR_UNSUPPORTED (-7)    /* option not compiled in this build */
+
+/* kernel versions, numbered as the reference's `kernel` argument
+ * (src/dspmv_mgpu_v1.cu:256-278) */
+#define SBLAS_KERNEL_ROWSPLIT 1       /* one sub-warp per row */
+#define SBLAS_KERNEL_MERGEPATH 2      /* nnz-balanced tiles, merge-path partition */
+#define SBLAS_KERNEL_CSR5 3           /* nnz-balanced tiles, CSR5 sigma rule */
+
+/* value storage of the matrix */
+#define SBLAS_VAL_F64 0
+#define SBLAS_VAL_F32 1               /* FP32 values, FP64 row sums */
+#define SBLAS_VAL_PATTERN 2           /* binary matrix, no value array */
+
+/* Message describing the last failure on this thread ("" if none). */
+SBLAS_API const char *sblas_last_error(void);
+/* Status code of the last call on this thread. */
+SBLAS_API int sblas_last_status(void);
+/* Library version string. */
+SBLAS_API const char *sblas_version(void);
+
+/* Reference-compatibility switches for the drop-in entry points (0 = off,
+ * the default: every entry point computes y = alpha*A*x + beta*y on all rows).
+ * 1 = reproduce the reference's observable results at ngpu = 1:
+ *   - nnz-split entry points (v1, v1_numa*, v2) leave rows before the first
+ *     and after the last non-empty row untouched;
+ *   - the CSC entry points and v1_numa(_coo) with merg_opt = 0 add the result
+ *     into the caller's y (y = y0 + alpha*A*x + beta*y0);
+ *   - kernel 3 (CSR5) computes y = A*x, ignoring alpha and beta.
+ * Process-wide; also set by the environment variable SBLAS_COMPAT=reference. */
+SBLAS_API void sblas_set_compat_mode(int mode);
+SBLAS_API int sblas_get_compat_mode(void);
+
+/* Bytes of device workspace the tile kernels of sblas_dcsrmv need for nnz nonzeros with
+ * tile parameter sigma (0 = library default). */
+SBLAS_API size_t sblas_tile_workspace_bytes(long long nnz, int sigma);
+
+/* Compiled tile shapes: sigma values usable below. */
+SBLAS_API int sblas_tile_sigma_count(void);
+SBLAS_API int sblas_tile_sigma_at(int i);
+/* Default sigma chosen for a matrix shape (kernel 2), and the sigma of the
+ * reference's CSR5 rule (kernel 3, include/anonymouslib_cuda.h:294-318). */
+SBLAS_API int sblas_default_sigma(int m, long long nnz);
+SBLAS_API int sblas_csr5_sigma(int m, long long nnz);
+
+/*
+ * y = alpha*A*x + beta*y, A in CSR on the device.  kernel: 1, 2 or 3.
+ * val_kind: SBLAS_VAL_F64 (val is double*), SBLAS_VAL_F32 (float*) or
+ * SBLAS_VAL_PATTERN (val ignored, every stored entry is 1.0); kernel 1 takes
+ * FP64 values only.  sigma: nonzeros per thread of the tile kernels
+ * (0 = default).  work/work_bytes: device workspace of at least
+ * sblas_tile_workspace_bytes(nnz, sigma) bytes, 256-byte aligned, or NULL to
+ * use a library-owned buffer (grown with cudaMalloc on first use; not
+ * usable inside CUDA-graph capture).  stream: a cudaStream_t (0 = legacy
+ * default stream).
+ */
+SBLAS_API int sblas_dcsrmv(int kernel, int m, int n, long long nnz, double alpha, const void *val,
+                 int val_kind, const int *rowptr, const int *col, const double *x,
+                 double beta, double *y, int sigma, void *work, size_t work_bytes,
+                 void *stream);
+
+/* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
+ * then runs the tile kernel.  rowptr_work: int[m + 1] device buffer. */
+SBLAS_API int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
+                 const int *coo_row, const int *coo_col, const double *x, double beta,
+                 double *y, int *rowptr_work, int sigma, void *work, size_t work_bytes,
+                 void *stream);
+
+/* CSC -> CSR on the device (stable; columns ascending inside each row).
+ * work: sblas_csc_to_csr_workspace_bytes(m, n, nnz) bytes. */
+SBLAS_API size_t sblas_csc_to_csr_workspace_bytes(int m, int n, long long nnz);
+SBLAS_API int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
+                     const int *csc_colptr, const int *csc_row, double *csr_val,
+                     int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,
+                     void *stream);
+
+/* Row-sorted COO row indices -> CSR row pointer (int[m + 1]). */
+SBLAS_API int sblas_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
+                             void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SBLAS_GB300_H */

@@ -215,6 +215,9 @@ int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
     for (int i = 0; i < nparts; i++)              /* :143-152 */
         end_row[i] = oracle_get_row_from_index(m, rowptr, end_idx[i]);
 
+    /* every part copies its rows of the caller's y before any merge (:242) */
+    double *y0 = (double *)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+    memcpy(y0, y, sizeof(double) * (size_t)m);
     for (int d = 0; d < nparts; d++) {
         int dm = end_row[d] - start_row[d] + 1;
         int dnnz = end_idx[d] - start_idx[d] + 1;
@@ -224,7 +227,7 @@ int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
         prow[dm] = dnnz;
         for (int j = 1; j < dm; j++) prow[j] = rowptr[start_row[d] + j] - start_idx[d];
         double *py = (double *)malloc(sizeof(double) * dm);
-        memcpy(py, y + start_row[d], sizeof(double) * dm);
+        memcpy(py, y0 + start_row[d], sizeof(double) * dm);
         oracle_csr_spmv(dm, n, dnnz, alpha, val + start_idx[d], prow, col + start_idx[d],
                         x, beta, py);
         /* :304-319 -- copy the part back, then for a row split with the
@@ -241,7 +244,7 @@ int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
         free(py);
     }
     free(start_idx); free(end_idx); free(start_row); free(end_row);
-    free(start_flag); free(y2);
+    free(start_flag); free(y2); free(y0);
     return 0;
 }
 
