@@ -1,0 +1,416 @@
+"""Benchmark of the FP64 SpMV hot path on GB300 (one JSON line on stdout).
+
+Workload (the power-law configuration): y = 1.0*A*x + 0.0*y, A a 4.0M x 4.0M
+power-law graph with ~70M nonzeros (out-degree exponent 2.1, max row 20k),
+values 1.0 FP64, x ~ U(0,1), int32 CSR indices.  One step = one SpMV over
+the whole matrix through sblas_dcsrmv (tile partition + tile kernel + carry
+fix-up; 3 launches), inputs resident in HBM.  The compulsory bytes (920 MB:
+val, col, rowptr, x read once, y written once) exceed the 129 MB L2, so no
+flush is needed between steps; x (32 MB) stays L2-resident by design.
+
+  value        compulsory GB/s of the whole job (all ranks) over the timed steps
+  e2e          same metric through the reference-facing C ABI
+               (spMV_mgpu_baseline) from pinned HOST buffers: host->device
+               copies of the matrix and x, the SpMV, the device->host copy of
+               y, all inside the timed region
+  roofline     the tile kernel (with its carry fix-up) timed alone with CUDA
+               events on its stream; peak = MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline the reference's CPU loop (oracle/_ref when built on this
+               machine, else its restatement in oracle/) on all host cores
+
+python bench.py --gpus N --steps K --warmup W [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SpMV HBM GB/s & % roofline: plain FP64 vs mixed/batched/fwd+bwd at stated err"
+WORKLOAD = ("power-law graph 4.0M x 4.0M, ~70M nnz (exponent 2.1, max row 20k), values 1.0 "
+            "FP64, x~U(0,1); FP64 CSR y=1.0*A*x+0.0*y")
+FALLBACK_HBM = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-extras", action="store_true", help="skip the other forms")
+    p.add_argument("--seed", type=int, default=2021)
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [s.strip() for s in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(device, seed):
+    from hpda_sblas_pnnl_gb300 import synth
+    a, x = synth.powerlaw(seed=seed, device=device)
+    return a, x
+
+
+def cpu_time_spmv(a_np, x_np, m, n, reps, threads, use_ref):
+    """Median seconds of the reference CPU loop on `threads` host threads."""
+    import numpy as np
+    from oracle import oracle as O
+    rp, col, val = a_np
+    y0 = np.zeros(m)
+    fn = (lambda: O.ref_csr_spmv(m, n, rp, col, val, x_np, y0, 1.0, 0.0, threads=threads)) \
+        if use_ref else \
+        (lambda: O.csr_spmv(m, n, rp, col, val, x_np, y0, 1.0, 0.0, threads=threads))
+    fn()
+    fn()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), ts
+
+
+def run_reference(args):
+    """--impl reference: the reference's own CPU SpMV (csr_spmv_cpu,
+    test/dspmv_test_smt.cu:39-52) on all host cores, same workload/metric."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from hpda_sblas_pnnl_gb300 import synth
+    from oracle import oracle as O
+    O.build() if not O.LIB.exists() else None
+    a, x = make_workload("cpu", args.seed)
+    m, n, nnz = a.m, a.n, a.nnz
+    a_np = tuple(np.ascontiguousarray(t) for t in a.numpy())
+    x_np = np.ascontiguousarray(x.numpy())
+    threads = os.cpu_count() or 1
+    use_ref = O.ref_available()
+    bytes_step = synth.compulsory_bytes(m, n, nnz)
+    med, ts = cpu_time_spmv(a_np, x_np, m, n, max(args.steps, 1), threads, use_ref)
+    # warmup and steps: every step is one full SpMV (a bounded sample: the
+    # whole matrix, ~0.1-1 s per step on the host)
+    total = sum(ts)
+    value = bytes_step * len(ts) / total / 1e9
+    kind = "reference" if use_ref else "port"
+    sample = f"full matrix ({nnz} nnz), {len(ts)} steps after 2 warm-up runs"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": ws, "steps": len(ts), "warmup": 2, "ms_per_step": round(1e3 * total / len(ts), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
+        "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
+                   "bytes_per_step": bytes_step, "host_threads": threads},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cuda_event_ms(fn, stream, reps):
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(reps)]
+    for e0, e1 in ev:
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from hpda_sblas_pnnl_gb300 import _lib, api, ops, synth
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load(build_if_missing=True)
+    stream = torch.cuda.current_stream(dev)
+
+    # each rank holds its own full-size instance (weak scaling, no collective
+    # on the data path): rank r uses seed + r
+    a, x = make_workload(dev, args.seed + rank)
+    m, n, nnz = a.m, a.n, a.nnz
+    y = torch.zeros(m, dtype=torch.float64, device=dev)
+    bytes_step = synth.compulsory_bytes(m, n, nnz)
+    kernel = ops.KERNEL_MERGEPATH
+    sigma = ops.default_sigma(m, nnz)
+    work = torch.empty(ops.workspace_bytes(nnz, sigma), dtype=torch.uint8, device=dev)
+
+    def step():
+        ops.csrmv(a.rowptr, a.col, a.val, x, y, 1.0, 0.0, kernel=kernel, sigma=sigma, work=work)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)  # let the sampler start before the timed region
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * bytes_step / (ms_step * 1e-3) / 1e9
+    launches_per_step = 3
+
+    # correctness of what was timed (oracle spot check on rank 0 is in the
+    # tests; here a cheap invariant: values are 1.0, so sum(y) = sum colcount*x)
+    cc = torch.bincount(a.col.to(torch.int64), minlength=n).to(torch.float64)
+    chk = abs(float(y.sum()) - float((cc * x).sum())) / float((cc * x).sum())
+
+    out = {}
+    if rank == 0:
+        # ---- roofline: tile kernel (+ carry fix-up) alone, analysed plan
+        plan = ops.CsrPlan(a.rowptr, a.col, a.val, kernel=kernel, sigma=sigma)
+        for _ in range(3):
+            plan(x, y)
+        kt = cuda_event_ms(lambda: plan(x, y), stream, 20)
+        k_ms = statistics.mean(kt)
+        pk, pk_kind = peaks()
+        achieved = bytes_step / (k_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk, "unit": "GB/s",
+                "frac": round(achieved / pk, 4), "traffic": None, "peak_source": pk_kind,
+                "kernel": f"tile_spmv_kernel<128,{sigma},F64> + tile_fixup_kernel",
+                "kernel_us": round(k_ms * 1e3, 2),
+                "fp64_note": "FP64 pipe measured at 5.04e11 DFMA/s; 1 DFMA per nonzero "
+                             f"caps this matrix at {5.04e11 * bytes_step / nnz / 1e9:.0f} GB/s"}
+        traffic_file = ROOT / "profiles" / "traffic.json"
+        if traffic_file.exists():
+            try:
+                tr = json.loads(traffic_file.read_text())
+                roof["traffic"] = tr.get("powerlaw_fp64_bytes_per_launch")
+            except Exception:
+                pass
+
+        # ---- e2e through the reference-facing C ABI with pinned host buffers
+        rp_h = a.rowptr.cpu().pin_memory().numpy()
+        col_h = a.col.cpu().pin_memory().numpy()
+        val_h = a.val.cpu().pin_memory().numpy()
+        x_h = x.cpu().pin_memory().numpy()
+        y_h = torch.zeros(m, dtype=torch.float64).pin_memory().numpy()
+        for _ in range(2):
+            api.spMV_mgpu_baseline(m, n, nnz, 1.0, val_h, rp_h, col_h, x_h, 0.0, y_h)
+        e2e_steps = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        rets = []
+        for _ in range(e2e_steps):
+            rets.append(api.spMV_mgpu_baseline(m, n, nnz, 1.0, val_h, rp_h, col_h, x_h, 0.0, y_h))
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        h2d = 8 * nnz + 4 * nnz + 4 * (m + 1) + 8 * n
+        d2h = 8 * m
+        e2e = {"value": round(bytes_step / e2e_s / 1e9, 3), "unit": "GB/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": round(e2e_s * 1e3, 3),
+               "comm_ms": round(1e3 * statistics.mean(r.comm_time for r in rets), 3),
+               "comp_ms": round(1e3 * statistics.mean(r.comp_time for r in rets), 3),
+               "api": "spMV_mgpu_baseline (include/spmv_kernel.h)"}
+        e2e_err = float(np.abs(y_h - y.cpu().numpy()).max())
+
+        # ---- CPU baseline (bounded sample: a few full SpMVs, all host cores)
+        cpu = None
+        if ws == 1:
+            from oracle import oracle as O
+            if not O.LIB.exists():
+                O.build()
+            threads = os.cpu_count() or 1
+            use_ref = O.ref_available()
+            a_np = (rp_h, col_h, val_h)
+            med, ts = cpu_time_spmv(a_np, x_h, m, n, 8, threads, use_ref)
+            cpu = {"value": round(bytes_step / med / 1e9, 3), "unit": "GB/s", "cores": threads,
+                   "kind": "reference" if use_ref else "port",
+                   "sample": f"8 full SpMVs of the same matrix (median), {threads} threads"}
+
+        extras = {}
+        if not args.no_extras:
+            extras = run_extras(dev, stream, args)
+
+        out = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
+            "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
+                       "bytes_per_step": bytes_step, "kernel": "2 (nnz tiles)", "sigma": sigma,
+                       "l2": "inputs larger than L2 (920 MB > 129 MB), no flush",
+                       "launches": "tile partition + tile kernel + carry fix-up",
+                       "check_rel_err": chk, "e2e_max_abs_diff": e2e_err},
+            "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        if extras:
+            out["forms"] = extras
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_extras(dev, stream, args):
+    """The other forms, each timed with CUDA events (kernel time, analysed
+    plan): banded FP64 and FP32-values, pattern-only power-law.  Errors are
+    relative L2 against the FP64 oracle's result on the same inputs."""
+    import numpy as np
+    import torch
+    from hpda_sblas_pnnl_gb300 import ops, synth
+    from oracle import oracle as O
+    pk, _ = peaks()
+    res = {}
+    threads = os.cpu_count() or 1
+
+    def timed(plan, x, y, reps=10):
+        for _ in range(3):
+            plan(x, y)
+        return statistics.mean(cuda_event_ms(lambda: plan(x, y), stream, reps))
+
+    a, x = synth.banded_fem(device=dev)
+    m, n, nnz = a.m, a.n, a.nnz
+    rp, c, v = a.numpy()
+    ref = O.csr_spmv(m, n, rp, c, v, x.cpu().numpy(), np.zeros(m), threads=threads)
+    nref = np.linalg.norm(ref)
+    y = torch.zeros(m, dtype=torch.float64, device=dev)
+    for name, val, vb in (("banded_fp64", a.val, 8), ("banded_fp32val", a.val.float(), 4)):
+        plan = ops.CsrPlan(a.rowptr, a.col, val)
+        ms = timed(plan, x, y)
+        err = float(np.linalg.norm(y.cpu().numpy() - ref) / nref)
+        b = synth.compulsory_bytes(m, n, nnz, val_bytes=vb)
+        res[name] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
+                     "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err, "nnz": nnz}
+        del plan
+    if "banded_fp64" in res and "banded_fp32val" in res:
+        res["fp32val_speedup"] = round(res["banded_fp64"]["us"] / res["banded_fp32val"]["us"], 3)
+    del a, x, y
+    torch.cuda.empty_cache()
+
+    a, x = synth.powerlaw(seed=args.seed, device=dev)
+    y = torch.zeros(a.m, dtype=torch.float64, device=dev)
+    plan = ops.CsrPlan(a.rowptr, a.col, None)
+    ms = timed(plan, x, y)
+    b = synth.compulsory_bytes(a.m, a.n, a.nnz, val_bytes=0)
+    rp, c, v = a.numpy()
+    ref = O.csr_spmv(a.m, a.n, rp, c, v, x.cpu().numpy(), np.zeros(a.m), threads=threads)
+    err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+    res["powerlaw_pattern"] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
+                               "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err}
+    # CSC and COO (device conversion once, then the tile kernel; conversion timed apart)
+    colptr, rowidx, cval = synth.csr_to_csc(a)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rp2, c2, v2 = ops.csc_to_csr(a.m, a.n, colptr, rowidx, cval)
+    torch.cuda.synchronize()
+    conv_ms = (time.perf_counter() - t0) * 1e3
+    row = synth.csr_to_coo_rows(a)
+    rpw = torch.empty(a.m + 1, dtype=torch.int32, device=dev)
+    coo_ms = statistics.mean(cuda_event_ms(
+        lambda: ops.coomv(row, a.col, a.val, x, y, rowptr_work=rpw), stream, 10))
+    bcoo = synth.compulsory_bytes(a.m, a.n, a.nnz, fmt="coo")
+    res["powerlaw_coo"] = {"gbs": round(bcoo / coo_ms / 1e6, 1),
+                           "frac": round(bcoo / coo_ms / 1e6 / pk, 4), "us": round(coo_ms * 1e3, 1),
+                           "note": "row pointer built on device each call, then tile kernel"}
+    res["powerlaw_csc_to_csr_ms"] = round(conv_ms, 2)
+    return res
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -51,6 +51,11 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_csr5_sigma": (C.c_int, [C.c_int, C.c_longlong]),
     "sblas_dcsrmv": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, C.c_int,
                                _vp, _vp, _vp, C.c_double, _vp, C.c_int, _vp, C.c_size_t, _vp]),
+    "sblas_csr_analyse": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, C.c_int, _vp,
+                                    C.c_size_t, _vp]),
+    "sblas_dcsrmv_analysed": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_double, _vp,
+                                        C.c_int, _vp, _vp, _vp, C.c_double, _vp, C.c_int, _vp,
+                                        C.c_size_t, _vp]),
     "sblas_dcoomv": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, _vp, _vp, _vp,
                                C.c_double, _vp, _vp, C.c_int, _vp, C.c_size_t, _vp]),
     "sblas_csc_to_csr_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_longlong]),

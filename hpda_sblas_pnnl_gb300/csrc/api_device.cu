@@ -178,6 +178,54 @@ int sblas_dcsrmv(int kernel, int m, int n, long long nnz, double alpha, const vo
                             work, st);
 }
 
+int sblas_csr_analyse(int kernel, int m, long long nnz, const int *rowptr, int sigma, void *work,
+                      size_t work_bytes, void *stream)
+{
+    clear_error();
+    if (m < 0 || nnz < 0 || nnz > 0x7fffffffLL || kernel < 2 || kernel > 3 || work == nullptr) {
+        set_error(SBLAS_ERR_ARG, "sblas_csr_analyse: bad arguments");
+        return SBLAS_ERR_ARG;
+    }
+    if (sigma <= 0)
+        sigma = (kernel == SBLAS_KERNEL_CSR5) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
+    if (work_bytes < tile_workspace_bytes(nnz, sigma) ||
+        (reinterpret_cast<uintptr_t>(work) & 255) != 0) {
+        set_error(SBLAS_ERR_ARG, "workspace needs %zu bytes at 256-byte alignment",
+                  tile_workspace_bytes(nnz, sigma));
+        return SBLAS_ERR_ARG;
+    }
+    return launch_tile_analyse(m, nnz, rowptr, sigma, work, static_cast<cudaStream_t>(stream));
+}
+
+int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, double alpha, const void *val,
+                          int val_kind, const int *rowptr, const int *col, const double *x,
+                          double beta, double *y, int sigma, void *work, size_t work_bytes,
+                          void *stream)
+{
+    clear_error();
+    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL || kernel < 2 || kernel > 3 ||
+        work == nullptr || val_kind < SBLAS_VAL_F64 || val_kind > SBLAS_VAL_PATTERN) {
+        set_error(SBLAS_ERR_ARG, "sblas_dcsrmv_analysed: bad arguments");
+        return SBLAS_ERR_ARG;
+    }
+    if (m == 0) return SBLAS_OK;
+    if (y == nullptr || (nnz > 0 && (rowptr == nullptr || col == nullptr || x == nullptr ||
+                                     (val_kind != SBLAS_VAL_PATTERN && val == nullptr)))) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    if (sigma <= 0)
+        sigma = (kernel == SBLAS_KERNEL_CSR5) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
+    if (work_bytes < tile_workspace_bytes(nnz, sigma) ||
+        (reinterpret_cast<uintptr_t>(work) & 255) != 0) {
+        set_error(SBLAS_ERR_ARG, "workspace needs %zu bytes at 256-byte alignment",
+                  tile_workspace_bytes(nnz, sigma));
+        return SBLAS_ERR_ARG;
+    }
+    return launch_tile_spmv(m, n, nnz, alpha, val, val_kind, rowptr, col, x, beta, y, sigma, work,
+                            static_cast<cudaStream_t>(stream), true);
+}
+
 int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
                  const int *coo_row, const int *coo_col, const double *x, double beta,
                  double *y, int *rowptr_work, int sigma, void *work, size_t work_bytes,

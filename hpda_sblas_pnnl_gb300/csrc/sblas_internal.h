@@ -50,9 +50,14 @@ enum ValueKind { VAL_F64 = 0, VAL_F32 = 1, VAL_PATTERN = 2 };
 
 // Launches partition + tile kernel + carry fix-up on `stream`.
 // `work` must hold tile_workspace_bytes(nnz, sigma) bytes, 256-byte aligned.
+// analysed = true: the partition of `work` was computed by
+// launch_tile_analyse for this row pointer and sigma (skipped here).
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
                      int val_kind, const int *rowptr, const int *col, const double *x,
-                     double beta, double *y, int sigma, void *work, cudaStream_t stream);
+                     double beta, double *y, int sigma, void *work, cudaStream_t stream,
+                     bool analysed = false);
+int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void *work,
+                        cudaStream_t stream);
 
 // Row-split kernel (one sub-warp per row; kernel version 1).
 int launch_rowsplit_spmv(int m, int n, long long nnz, double alpha, const double *val,

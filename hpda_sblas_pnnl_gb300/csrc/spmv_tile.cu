@@ -530,9 +530,32 @@ int launch_scale_y(int m, double beta, double *y, cudaStream_t stream)
     return SBLAS_OK;
 }
 
+int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void *work,
+                        cudaStream_t stream)
+{
+    if (m <= 0 || nnz <= 0) return SBLAS_OK;
+    if (tile_shape_index(sigma) < 0) {
+        set_error(SBLAS_ERR_UNSUPPORTED, "sigma %d is not a compiled tile shape", sigma);
+        return SBLAS_ERR_UNSUPPORTED;
+    }
+    const long long tile = (long long)kThreads * sigma;
+    const long long ntiles_ll = (nnz + tile - 1) / tile;
+    if (ntiles_ll > INT_MAX - 2) {
+        set_error(SBLAS_ERR_ARG, "nnz %lld too large", nnz);
+        return SBLAS_ERR_ARG;
+    }
+    const int ntiles = (int)ntiles_ll;
+    int *part = static_cast<int *>(work);
+    const int threads = 256;
+    const int blocks = (ntiles + 1 + threads - 1) / threads;
+    tile_partition_kernel<<<blocks, threads, 0, stream>>>(m, nnz, ntiles, tile, rowptr, part);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val, int val_kind,
                      const int *rowptr, const int *col, const double *x, double beta, double *y,
-                     int sigma, void *work, cudaStream_t stream)
+                     int sigma, void *work, cudaStream_t stream, bool analysed)
 {
     if (m <= 0) return SBLAS_OK;
     if (nnz <= 0) return launch_scale_y(m, beta, y, stream);
@@ -553,11 +576,9 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     int *status = reinterpret_cast<int *>(w + align256(sizeof(int) * (size_t)(ntiles + 1)) +
                                           align256(sizeof(double) * (size_t)ntiles));
     SBLAS_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
-    {
-        const int threads = 256;
-        const int blocks = (ntiles + 1 + threads - 1) / threads;
-        tile_partition_kernel<<<blocks, threads, 0, stream>>>(m, nnz, ntiles, tile, rowptr, part);
-        SBLAS_CUDA_TRY(cudaGetLastError());
+    if (!analysed) {
+        const int rc = launch_tile_analyse(m, nnz, rowptr, sigma, work, stream);
+        if (rc != SBLAS_OK) return rc;
     }
     TileArgs a;
     a.m = m;

@@ -134,3 +134,55 @@ def cscmv(colptr: torch.Tensor, rowidx: torch.Tensor, val: torch.Tensor, x: torc
     n = colptr.numel() - 1
     rp, c, v = csc_to_csr(m, n, colptr, rowidx, val)
     return csrmv(rp, c, v, x, y, alpha, beta, n=n)
+
+
+class CsrPlan:
+    """A CSR matrix analysed once for repeated products (kernel 2 or 3).
+
+    The tile partition of the row pointer is computed at construction
+    (sblas_csr_analyse) into a workspace owned by the plan; each call runs
+    only the tile kernel and the carry fix-up (sblas_dcsrmv_analysed), does
+    not allocate and can be captured in a CUDA graph.
+    """
+
+    def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
+                 n: int | None = None, kernel: int = KERNEL_MERGEPATH, sigma: int = 0):
+        dev = _require_cuda(rowptr, col, val)
+        if kernel not in (KERNEL_MERGEPATH, KERNEL_CSR5):
+            raise ValueError("plans use the tile kernels (2 or 3)")
+        lib = _lib.load()
+        self.rowptr, self.col, self.val = rowptr, col, val
+        self.m = rowptr.numel() - 1
+        self.nnz = col.numel()
+        self.n = int(n) if n is not None else None
+        self.kernel = kernel
+        if sigma <= 0:
+            sigma = (lib.sblas_csr5_sigma(self.m, self.nnz) if kernel == KERNEL_CSR5
+                     else lib.sblas_default_sigma(self.m, self.nnz))
+        self.sigma = int(sigma)
+        if val is None:
+            self.vk = VAL_PATTERN
+        elif val.dtype == torch.float64:
+            self.vk = VAL_F64
+        elif val.dtype == torch.float32:
+            self.vk = VAL_F32
+        else:
+            raise TypeError("val must be float64, float32 or None")
+        self.work_bytes = int(lib.sblas_tile_workspace_bytes(self.nnz, self.sigma))
+        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=dev)
+        self.device = dev
+        with torch.cuda.device(dev):
+            rc = lib.sblas_csr_analyse(kernel, self.m, self.nnz, _ptr(rowptr), self.sigma,
+                                       _ptr(self.work), self.work_bytes, _stream_ptr(dev))
+        _lib.check(rc)
+
+    def __call__(self, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0,
+                 beta: float = 0.0) -> torch.Tensor:
+        n = self.n if self.n is not None else x.numel()
+        lib = _lib.load()
+        rc = lib.sblas_dcsrmv_analysed(self.kernel, self.m, n, self.nnz, float(alpha),
+                                       _ptr(self.val), self.vk, _ptr(self.rowptr), _ptr(self.col),
+                                       _ptr(x), float(beta), _ptr(y), self.sigma, _ptr(self.work),
+                                       self.work_bytes, _stream_ptr(self.device))
+        _lib.check(rc)
+        return y

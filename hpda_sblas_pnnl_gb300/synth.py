@@ -140,9 +140,8 @@ def banded_fem(m: int = 2_000_000, per_row: int = 140, band: int = 20_000, offba
     always present), plus `offband` x per_row random entries per row anywhere.
     Values ~ N(0, 1), diagonal set to 1 + sum of |off-diagonal| of its row
     (diagonally dominant), x ~ N(0, 1)."""
-    assert m % 3 == 0
     g = _gen(seed, device)
-    nb = m // 3
+    nb = (m + 2) // 3  # the last block row may be partial
     half = band // 6  # block columns on each side of the diagonal block
     bpr = max(1, round(per_row * (1 - offband) / 3))  # blocks per block row
     br = torch.arange(nb, device=device).repeat_interleave(bpr)
@@ -154,6 +153,9 @@ def banded_fem(m: int = 2_000_000, per_row: int = 140, band: int = 20_000, offba
     rows = (3 * br[:, None, None] + a[None, :, None]).expand(-1, 3, 3).reshape(-1)
     cols = (3 * bc[:, None, None] + a[None, None, :]).expand(-1, 3, 3).reshape(-1)
     del br, off, bc
+    if m % 3:
+        keep = (rows < m) & (cols < m)
+        rows, cols = rows[keep], cols[keep]
     n_off = int(round(per_row * offband * m))
     if n_off > 0:
         ro = torch.randint(0, m, (n_off,), generator=g, device=device)

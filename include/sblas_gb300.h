@@ -96,6 +96,18 @@ SBLAS_API int sblas_dcsrmv(int kernel, int m, int n, long long nnz, double alpha
                  double beta, double *y, int sigma, void *work, size_t work_bytes,
                  void *stream);
 
+/* Analysis / execution split of the tile kernels (kernel 2 or 3) for a
+ * matrix used many times: sblas_csr_analyse writes the tile partition of the
+ * row pointer into `work`; sblas_dcsrmv_analysed then runs only the tile
+ * kernel and the carry fix-up, reusing it (same rowptr, nnz, sigma and
+ * work).  Neither allocates, so both can be captured in a CUDA graph. */
+SBLAS_API int sblas_csr_analyse(int kernel, int m, long long nnz, const int *rowptr, int sigma,
+                                void *work, size_t work_bytes, void *stream);
+SBLAS_API int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, double alpha,
+                                    const void *val, int val_kind, const int *rowptr,
+                                    const int *col, const double *x, double beta, double *y,
+                                    int sigma, void *work, size_t work_bytes, void *stream);
+
 /* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
  * then runs the tile kernel.  rowptr_work: int[m + 1] device buffer. */
 SBLAS_API int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
