@@ -48,6 +48,11 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-extras", action="store_true", help="skip the other forms")
     p.add_argument("--seed", type=int, default=2021)
+    p.add_argument("--m", type=int, default=4_000_000,
+                   help="rows of the power-law matrix (smaller only for profiling captures)")
+    p.add_argument("--kernel-only", action="store_true",
+                   help="time the device steps only (no e2e, CPU baseline, extras): the "
+                        "small case used for ncu captures")
     return p.parse_args()
 
 
@@ -114,9 +119,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(device, seed):
+def make_workload(device, seed, m=4_000_000):
     from hpda_sblas_pnnl_gb300 import synth
-    a, x = synth.powerlaw(seed=seed, device=device)
+    a, x = synth.powerlaw(m=m, seed=seed, device=device)
     return a, x
 
 
@@ -207,7 +212,7 @@ def run_ours(args):
 
     # each rank holds its own full-size instance (weak scaling, no collective
     # on the data path): rank r uses seed + r
-    a, x = make_workload(dev, args.seed + rank)
+    a, x = make_workload(dev, args.seed + rank, args.m)
     m, n, nnz = a.m, a.n, a.nnz
     y = torch.zeros(m, dtype=torch.float64, device=dev)
     bytes_step = synth.compulsory_bytes(m, n, nnz)
@@ -253,7 +258,14 @@ def run_ours(args):
     chk = abs(float(y.sum()) - float((cc * x).sum())) / float((cc * x).sum())
 
     out = {}
-    if rank == 0:
+    if rank == 0 and args.kernel_only:
+        print(json.dumps({"metric": METRIC, "value": round(value, 2), "unit": "GB/s",
+                          "n_gpus": ws, "steps": args.steps, "ms_per_step": round(ms_step, 4),
+                          "config": {"m": m, "nnz": nnz, "sigma": sigma,
+                                     "bytes_per_step": bytes_step},
+                          "note": "kernel-only small case (profiling); not the benchmark line"}),
+              flush=True)
+    elif rank == 0:
         # ---- roofline: tile kernel (+ carry fix-up) alone, analysed plan
         plan = ops.CsrPlan(a.rowptr, a.col, a.val, kernel=kernel, sigma=sigma)
         for _ in range(3):

@@ -105,6 +105,17 @@ __device__ __forceinline__ double ldg_x(const double *p, uint64_t policy)
     return v;
 }
 
+// Same load, kept in program order (volatile): used to issue all gathers
+// of a thread's chunk before the dependent FMA chain consumes them.
+__device__ __forceinline__ double ldg_x_issue(const double *p, uint64_t policy)
+{
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;"
+                 : "=d"(v)
+                 : "l"(p), "l"(policy));
+    return v;
+}
+
 __device__ __forceinline__ float2 ldg_x2(const float2 *p, uint64_t policy)
 {
     float2 v;

@@ -228,10 +228,18 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
             const bool starts_before = (long long)rp(r) < s0;
             long long next = rp(r + 1);
             bool first_seg = true;
+            // issue every gather of the chunk first (one L2 round trip per
+            // chunk instead of one per nonzero), then run the FMA chain
             double xv[SIGMA];
+            if (cnt == SIGMA) {
 #pragma unroll
-            for (int j = 0; j < SIGMA; ++j)
-                xv[j] = (j < cnt) ? ptx::ldg_x(a.x + cst[c0 + j], pol_x) : 0.0;
+                for (int j = 0; j < SIGMA; ++j)
+                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + j], pol_x);
+            } else {
+#pragma unroll
+                for (int j = 0; j < SIGMA; ++j)
+                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + (j < cnt ? j : 0)], pol_x);
+            }
 #pragma unroll
             for (int j = 0; j < SIGMA; ++j) {
                 const long long k = s0 + j;
