@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--seed", type=int, default=2021)
     p.add_argument("--m", type=int, default=4_000_000,
                    help="rows of the power-law matrix (smaller only for profiling captures)")
+    p.add_argument("--sigma", type=int, default=0, help="tile shape (0 = library default)")
     p.add_argument("--kernel-only", action="store_true",
                    help="time the device steps only (no e2e, CPU baseline, extras): the "
                         "small case used for ncu captures")
@@ -217,7 +218,7 @@ def run_ours(args):
     y = torch.zeros(m, dtype=torch.float64, device=dev)
     bytes_step = synth.compulsory_bytes(m, n, nnz)
     kernel = ops.KERNEL_MERGEPATH
-    sigma = ops.default_sigma(m, nnz)
+    sigma = args.sigma if args.sigma > 0 else ops.default_sigma(m, nnz)
     work = torch.empty(ops.workspace_bytes(nnz, sigma), dtype=torch.uint8, device=dev)
 
     def step():

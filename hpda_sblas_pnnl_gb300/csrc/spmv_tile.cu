@@ -76,7 +76,8 @@ struct Layout {
     static constexpr size_t CIN = TAILV + size_t(THREADS) * 8;
     static constexpr size_t TAILK = CIN + size_t(THREADS) * 8;
     static constexpr size_t HEADK = TAILK + size_t(THREADS) * 4;
-    static constexpr size_t BAR = align16(HEADK + size_t(THREADS) * 4);
+    static constexpr size_t HEADV = align16(HEADK + size_t(THREADS) * 4);
+    static constexpr size_t BAR = align16(HEADV + size_t(THREADS) * 8);
     static constexpr size_t TOTAL = BAR + STAGES * 8;
 };
 
@@ -147,6 +148,7 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
     double *cin_s = reinterpret_cast<double *>(smem + L::CIN);
     int *tailk_s = reinterpret_cast<int *>(smem + L::TAILK);
     int *headk_s = reinterpret_cast<int *>(smem + L::HEADK);
+    double *headv_s = reinterpret_cast<double *>(smem + L::HEADV);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::BAR);
 
     const int tid = threadIdx.x;
@@ -209,28 +211,19 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         // ---------------- per-thread chunk: SIGMA consecutive nonzeros ----------
         const int c0 = tid * SIGMA;                          // local offset in tile
         const int cnt = max(0, min(SIGMA, cnt_tile - c0));
-        const long long s0 = tb + c0;                        // global nnz index
+        const int s0 = (int)(tb + c0);                       // global nnz index
         auto rp = [&](int r) -> int {                        // rowptr[r], r in [R0, R1+1]
             return fits ? rptr_s[r - R0] : __ldg(a.rowptr + r);
         };
-        double sum = 0.0;
-        int r = R0;
-        int head_row = -1;
-        double head_val = 0.0;
+        double xv[SIGMA];
+        int r0 = R0, rl = R0;      // rows of the chunk's first and last nonzero
+        bool sb = false;           // the first row began before the chunk
+        unsigned mask = 0;         // bit j: nonzero j of the chunk starts a new row
+        bool slow = !fits;         // empty rows inside the chunk, or rows not in smem
         if (cnt > 0) {
-            // last row r in [R0, R1] with rowptr[r] <= s0
-            int lo = R0, hi = min(R1, a.m - 1);
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if ((long long)rp(mid) <= s0) lo = mid; else hi = mid - 1;
-            }
-            r = lo;
-            const bool starts_before = (long long)rp(r) < s0;
-            long long next = rp(r + 1);
-            bool first_seg = true;
             // issue every gather of the chunk first (one L2 round trip per
-            // chunk instead of one per nonzero), then run the FMA chain
-            double xv[SIGMA];
+            // chunk instead of one per nonzero); the row search below runs
+            // while they are in flight
             if (cnt == SIGMA) {
 #pragma unroll
                 for (int j = 0; j < SIGMA; ++j)
@@ -240,13 +233,64 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
                 for (int j = 0; j < SIGMA; ++j)
                     xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + (j < cnt ? j : 0)], pol_x);
             }
+            // last row r in [R0, R1] with rowptr[r] <= s0
+            int lo = R0, hi = min(R1, a.m - 1);
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rp(mid) <= s0) lo = mid; else hi = mid - 1;
+            }
+            r0 = lo;
+            sb = rp(r0) < s0;
+            // row starts strictly inside the chunk -> boundary bits
+            int rr = r0, nx = rp(r0 + 1);
+            const int send = s0 + cnt;
+            while (nx < send) {
+                mask |= 1u << (nx - s0);
+                const int n2 = rp(rr + 2);
+                slow |= (n2 == nx);   // an empty row follows: general path
+                ++rr;
+                nx = n2;
+            }
+            rl = rr;
+        }
+        const bool warp_slow = __any_sync(0xffffffffu, slow);
+        double sum = 0.0;
+        int head_row = -1;
+        double head_val = 0.0;
+        if (cnt > 0 && !warp_slow) {
+            // branch-free FMA chain: at a row start the running sum is stored
+            // (the first segment to the thread's head slot when the row began
+            // in an earlier chunk) and restarted with a select
+            double *dst = sb ? &headv_s[tid] : &rval_s[r0 - R0];
+            double *nxt = &rval_s[r0 + 1 - R0];
 #pragma unroll
             for (int j = 0; j < SIGMA; ++j) {
-                const long long k = s0 + j;
+                const bool b = (mask >> j) & 1u;
+                if (b) *dst = sum;
+                dst = b ? nxt : dst;
+                nxt = b ? nxt + 1 : nxt;
+                sum = b ? 0.0 : sum;
+                if (j < cnt) {
+                    if (VK == VAL_PATTERN) sum += xv[j];
+                    else sum = fma((double)vst[c0 + j], xv[j], sum);
+                }
+            }
+            if (sb && mask != 0u) {
+                head_row = r0;
+                head_val = headv_s[tid];
+            }
+        } else if (cnt > 0) {
+            // general path: empty rows, or row pointer read from global memory
+            int r = r0;
+            int next = rp(r + 1);
+            bool first_seg = true;
+#pragma unroll
+            for (int j = 0; j < SIGMA; ++j) {
+                const int k = s0 + j;
                 if (j < cnt && k == next) {
                     // row r ended at k-1: a head (row began in an earlier chunk)
                     // or a complete row; restart the running sum
-                    if (first_seg && starts_before) {
+                    if (first_seg && sb) {
                         head_row = r;
                         head_val = sum;
                     } else if (fits) {
@@ -264,16 +308,13 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
                     }
                 }
                 if (j < cnt) {
-                    const double v = (VK == VAL_PATTERN) ? 1.0 : (double)vst[c0 + j];
-                    sum = (VK == VAL_PATTERN) ? sum + xv[j] : fma(v, xv[j], sum);
+                    if (VK == VAL_PATTERN) sum += xv[j];
+                    else sum = fma((double)vst[c0 + j], xv[j], sum);
                 }
             }
-            tailv_s[tid] = sum;
-            tailk_s[tid] = r;
-        } else {
-            tailv_s[tid] = 0.0;
-            tailk_s[tid] = -1;  // no data: never emitted
         }
+        tailv_s[tid] = sum;
+        tailk_s[tid] = (cnt > 0) ? rl : -1;   // -1: no data, never emitted
         headk_s[tid] = head_row;
         __syncthreads();  // B2: tails/heads published; stage s no longer read
 
