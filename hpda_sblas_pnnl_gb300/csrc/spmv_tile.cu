@@ -66,12 +66,15 @@ struct ValTraits<VAL_PATTERN> {
 template <int THREADS, int SIGMA, int VK>
 struct Layout {
     static constexpr int TILE = THREADS * SIGMA;
-    static constexpr int RCAP = TILE + 2;  // rowptr entries held in shared memory
+    static constexpr int RCAP = TILE + 2;       // rows (+2) of a tile that fit in smem
+    static constexpr int RSLOT = (RCAP + 8 + 3) / 4 * 4;  // per-stage row-pointer slot,
+                                                           // 16-byte multiple with slack
     static constexpr int VB = ValTraits<VK>::BYTES;
     static constexpr size_t VAL = 0;
     static constexpr size_t COL = align16(VAL + size_t(STAGES) * TILE * VB);
     static constexpr size_t RPTR = align16(COL + size_t(STAGES) * TILE * 4);
-    static constexpr size_t RVAL = align16(RPTR + size_t(RCAP) * 4);
+    static constexpr size_t META = align16(RPTR + size_t(STAGES) * RSLOT * 4);
+    static constexpr size_t RVAL = align16(META + size_t(STAGES) * 4 * 4);
     static constexpr size_t TAILV = align16(RVAL + size_t(RCAP) * 8);
     static constexpr size_t CIN = TAILV + size_t(THREADS) * 8;
     static constexpr size_t TAILK = CIN + size_t(THREADS) * 8;
@@ -96,7 +99,8 @@ struct TileArgs {
     const int *row_part;  // [ntiles + 1]
     double *carry;        // [ntiles]
     int *status;          // [1]
-    int use_tma;
+    int use_tma;          // val and col 16-byte aligned: bulk copies
+    int rp_tma;           // rowptr 16-byte aligned: bulk copies of its tile slices
 };
 
 // y epilogue for one finished row value v.
@@ -109,26 +113,50 @@ __device__ __forceinline__ double finish_row(double v, double alpha, double beta
     return fma(alpha, v, beta * __ldg(yp));              // general
 }
 
-// Issues the bulk copies of tile `tile` into stage `s` (one thread).
+// Stages tile `tile` into stage `s` (one producer thread): its owned-row
+// range (R0, R1) from the partition (passed in, prefetched by the caller),
+// val and col by bulk copy, and the row-pointer slice rowptr[R0 .. R1+1] by
+// bulk copy of its 16-byte-aligned superset (a few entries at the very end of
+// the array by plain loads).  All completes on the stage's mbarrier.
 template <int THREADS, int SIGMA, int VK>
 __device__ __forceinline__ void issue_tile(const TileArgs &a, unsigned char *smem, int tile,
-                                           int s, uint64_t pol)
+                                           int s, int R0, int R1, uint64_t pol)
 {
     using L = Layout<THREADS, SIGMA, VK>;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::BAR) + s;
+    int *meta = reinterpret_cast<int *>(smem + L::META) + 4 * s;
+    int *rslot = reinterpret_cast<int *>(smem + L::RPTR) + size_t(s) * L::RSLOT;
     const long long tb = (long long)tile * L::TILE;
     const long long cnt = (a.nnz - tb < L::TILE) ? (a.nnz - tb) : L::TILE;
-    uint32_t vbytes = 0, cbytes = 0;
+    uint32_t vbytes = 0, cbytes = 0, rbytes = 0;
     if (a.use_tma) {
         vbytes = (uint32_t)((cnt * L::VB) & ~15ll);
         cbytes = (uint32_t)((cnt * 4) & ~15ll);
     }
-    ptx::mbar_arrive_expect_tx(bar, vbytes + cbytes);
+    const int nr = R1 - R0;
+    const int fits = (nr + 2) <= L::RCAP;
+    int base = R0;
+    if (fits && a.rp_tma) {
+        const int count = min(nr + 2, a.m - R0 + 1);   // rowptr[R0 .. R0+count-1]
+        const int a0 = R0 & ~3;
+        const int a1 = R0 + count;
+        const int safe_end = (a.m + 1) & ~3;            // bulk copies stay inside rowptr
+        const int t_end = max(a0, min((a1 + 3) & ~3, safe_end));
+        base = a0;
+        rbytes = (uint32_t)(t_end - a0) * 4u;
+        for (int i = t_end; i < a1; ++i) rslot[i - a0] = __ldg(a.rowptr + i);
+    }
+    meta[0] = R0;
+    meta[1] = R1;
+    meta[2] = base;
+    meta[3] = fits;
+    ptx::mbar_arrive_expect_tx(bar, vbytes + cbytes + rbytes);   // release: meta, plain loads
     if (vbytes)
         ptx::bulk_g2s(smem + L::VAL + size_t(s) * L::TILE * L::VB,
                       static_cast<const unsigned char *>(a.val) + tb * L::VB, vbytes, bar, pol);
     if (cbytes)
         ptx::bulk_g2s(smem + L::COL + size_t(s) * L::TILE * 4, a.col + tb, cbytes, bar, pol);
+    if (rbytes) ptx::bulk_g2s(rslot, a.rowptr + base, rbytes, bar, pol);
 }
 
 template <int THREADS, int SIGMA, int VK, int AB>
@@ -142,7 +170,8 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
     extern __shared__ __align__(128) unsigned char smem[];
     VT *val_s = reinterpret_cast<VT *>(smem + L::VAL);
     int *col_s = reinterpret_cast<int *>(smem + L::COL);
-    int *rptr_s = reinterpret_cast<int *>(smem + L::RPTR);
+    int *rptr_base = reinterpret_cast<int *>(smem + L::RPTR);
+    const int *meta_s = reinterpret_cast<const int *>(smem + L::META);
     double *rval_s = reinterpret_cast<double *>(smem + L::RVAL);
     double *tailv_s = reinterpret_cast<double *>(smem + L::TAILV);
     double *cin_s = reinterpret_cast<double *>(smem + L::CIN);
@@ -161,11 +190,14 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         for (int s = 0; s < STAGES; ++s) ptx::mbar_init(bar + s, 1);
         ptx::fence_mbar_init();
     }
+    for (int i = tid; i < L::RCAP; i += THREADS) rval_s[i] = 0.0;  // kept zero between tiles
     __syncthreads();
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) {
             const int t = blockIdx.x + s * gridDim.x;
-            if (t < a.ntiles) issue_tile<THREADS, SIGMA, VK>(a, smem, t, s, pol_stream);
+            if (t < a.ntiles)
+                issue_tile<THREADS, SIGMA, VK>(a, smem, t, s, __ldg(a.row_part + t),
+                                               __ldg(a.row_part + t + 1), pol_stream);
         }
     }
 
@@ -174,20 +206,18 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
     for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
         const int s = it % STAGES;
         const uint32_t parity = (uint32_t)((it / STAGES) & 1);
-        const int R0 = __ldg(a.row_part + tile);
-        const int R1 = __ldg(a.row_part + tile + 1);
         const long long tb = (long long)tile * TILE;
         const int cnt_tile = (int)((a.nnz - tb < TILE) ? (a.nnz - tb) : TILE);
-        const int nr = R1 - R0;                       // rows owned by this tile
-        const bool fits = (nr + 2) <= L::RCAP;        // CTA-uniform
         VT *vst = val_s + size_t(s) * TILE;
         int *cst = col_s + size_t(s) * TILE;
-
-        // rows R0 .. R1 (+1 for the end pointer) of the row pointer
-        if (fits) {
-            const int nload = min(nr + 2, a.m - R0 + 1);
-            for (int i = tid; i < nload; i += THREADS) rptr_s[i] = __ldg(a.rowptr + R0 + i);
-            for (int i = tid; i < nr; i += THREADS) rval_s[i] = 0.0;
+        int *rptr_s = rptr_base + size_t(s) * L::RSLOT;
+        // the producer prefetches the partition entries of the tile it will
+        // stage after this one's data is consumed
+        const int nt = tile + STAGES * (int)gridDim.x;
+        int nR0 = 0, nR1 = 0;
+        if (tid == 0 && nt < a.ntiles) {
+            nR0 = __ldg(a.row_part + nt);
+            nR1 = __ldg(a.row_part + nt + 1);
         }
         cin_s[tid] = 0.0;
         if (tid == 0) a.carry[tile] = 0.0;
@@ -201,8 +231,17 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
             for (int i = cdone + tid; i < cnt_tile; i += THREADS) cst[i] = __ldg(a.col + tb + i);
         }
         const bool arrived = ptx::mbar_wait_bounded(bar + s, parity, WAIT_LIMIT_NS);
-        // B1: tile data, row pointer and cleared row sums visible; a timed-out
-        // wait anywhere in the CTA stops the CTA (uniform decision)
+        const int R0 = meta_s[4 * s + 0];
+        const int R1 = meta_s[4 * s + 1];
+        const int rbase = meta_s[4 * s + 2];
+        const bool fits = meta_s[4 * s + 3] != 0;     // CTA-uniform
+        const int nr = R1 - R0;                        // rows owned by this tile
+        if (arrived && fits && !a.rp_tma) {
+            const int nload = min(nr + 2, a.m - R0 + 1);
+            for (int i = tid; i < nload; i += THREADS) rptr_s[i] = __ldg(a.rowptr + R0 + i);
+        }
+        // B1: tile data and row pointer visible; a timed-out wait anywhere in
+        // the CTA stops the CTA (uniform decision)
         if (__syncthreads_or(!arrived)) {
             if (tid == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
             break;
@@ -213,7 +252,7 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         const int cnt = max(0, min(SIGMA, cnt_tile - c0));
         const int s0 = (int)(tb + c0);                       // global nnz index
         auto rp = [&](int r) -> int {                        // rowptr[r], r in [R0, R1+1]
-            return fits ? rptr_s[r - R0] : __ldg(a.rowptr + r);
+            return fits ? rptr_s[r - rbase] : __ldg(a.rowptr + r);
         };
         double xv[SIGMA];
         int r0 = R0, rl = R0;      // rows of the chunk's first and last nonzero
@@ -318,12 +357,9 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         headk_s[tid] = head_row;
         __syncthreads();  // B2: tails/heads published; stage s no longer read
 
-        if (tid == 0) {
-            const int nt = tile + STAGES * (int)gridDim.x;
-            if (nt < a.ntiles) {
-                ptx::fence_proxy_async_smem();
-                issue_tile<THREADS, SIGMA, VK>(a, smem, nt, s, pol_stream);
-            }
+        if (tid == 0 && nt < a.ntiles) {
+            ptx::fence_proxy_async_smem();
+            issue_tile<THREADS, SIGMA, VK>(a, smem, nt, s, nR0, nR1, pol_stream);
         }
 
         // ---------------- carry pass: reduce runs of tails (warp 0) ------------
@@ -397,15 +433,18 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         __syncthreads();  // B4: row sums final
 
         if (fits) {
-            for (int i = tid; i < nr; i += THREADS)
+            // finished rows out (coalesced); the row-sum slots are cleared for
+            // the next tile, which writes them only after its B1
+            for (int i = tid; i < nr; i += THREADS) {
                 a.y[R0 + i] = finish_row<AB>(rval_s[i], alpha, beta, a.y + R0 + i);
+                rval_s[i] = 0.0;
+            }
         } else {
             // rows without nonzeros were skipped above; write them here
             for (int rr = R0 + tid; rr < R1; rr += THREADS)
                 if (__ldg(a.rowptr + rr) == __ldg(a.rowptr + rr + 1))
                     a.y[rr] = finish_row<AB>(0.0, alpha, beta, a.y + rr);
         }
-        __syncthreads();  // B5: shared buffers free for the next tile
     }
 
     // drain: a tile whose copies were issued but not consumed (early exit)
@@ -548,7 +587,7 @@ int default_sigma_for(int m, long long nnz)
 {
     (void)m;
     (void)nnz;
-    return 23;
+    return 19;
 }
 
 int csr5_sigma_for(int m, long long nnz)
@@ -646,6 +685,7 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     a.status = status;
     const uintptr_t vb = reinterpret_cast<uintptr_t>(val), cb = reinterpret_cast<uintptr_t>(col);
     a.use_tma = ((val_kind == VAL_PATTERN || (vb & 15) == 0) && (cb & 15) == 0) ? 1 : 0;
+    a.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
     int rc = SBLAS_OK;
     switch (sigma) {
     case 7: rc = launch_vk<7>(val_kind, a, stream); break;
