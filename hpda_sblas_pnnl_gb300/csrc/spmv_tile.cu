@@ -63,25 +63,33 @@ struct ValTraits<VAL_PATTERN> {
     static constexpr int BYTES = 0;
 };
 
-template <int THREADS, int SIGMA, int VK>
+constexpr int NCW = 4;                 // compute warps per CTA
+constexpr int TC = NCW * 32;           // compute threads per CTA (one chunk each)
+constexpr int CTA_THREADS = TC + 32;   // + one service warp
+
+template <int SIGMA, int VK>
 struct Layout {
-    static constexpr int TILE = THREADS * SIGMA;
-    static constexpr int RCAP = TILE + 2;       // rows (+2) of a tile that fit in smem
-    static constexpr int RSLOT = (RCAP + 8 + 3) / 4 * 4;  // per-stage row-pointer slot,
-                                                           // 16-byte multiple with slack
+    static constexpr int TILE = TC * SIGMA;
+    static constexpr int RCAP = TILE / 4 + 2;   // owned rows (+2) of a tile held in smem;
+                                                // denser tiles use the global-memory path
+    static constexpr int RSLOT = (RCAP + 8 + 3) / 4 * 4;  // per-stage row-pointer slot
     static constexpr int VB = ValTraits<VK>::BYTES;
+    // staged tiles
     static constexpr size_t VAL = 0;
     static constexpr size_t COL = align16(VAL + size_t(STAGES) * TILE * VB);
     static constexpr size_t RPTR = align16(COL + size_t(STAGES) * TILE * 4);
     static constexpr size_t META = align16(RPTR + size_t(STAGES) * RSLOT * 4);
-    static constexpr size_t RVAL = align16(META + size_t(STAGES) * 4 * 4);
-    static constexpr size_t TAILV = align16(RVAL + size_t(RCAP) * 8);
-    static constexpr size_t CIN = TAILV + size_t(THREADS) * 8;
-    static constexpr size_t TAILK = CIN + size_t(THREADS) * 8;
-    static constexpr size_t HEADK = TAILK + size_t(THREADS) * 4;
-    static constexpr size_t HEADV = align16(HEADK + size_t(THREADS) * 4);
-    static constexpr size_t BAR = align16(HEADV + size_t(THREADS) * 8);
-    static constexpr size_t TOTAL = BAR + STAGES * 8;
+    // carry buffers, double-buffered by tile parity
+    static constexpr size_t RVAL = align16(META + size_t(STAGES) * 16);
+    static constexpr size_t TAILV = align16(RVAL + 2 * size_t(RCAP) * 8);
+    static constexpr size_t HEADV = TAILV + 2 * size_t(TC) * 8;
+    static constexpr size_t CIN = HEADV + 2 * size_t(TC) * 8;
+    static constexpr size_t TAILK = CIN + size_t(TC) * 8;
+    static constexpr size_t HEADK = TAILK + 2 * size_t(TC) * 4;
+    static constexpr size_t CMETA = align16(HEADK + 2 * size_t(TC) * 4);
+    // mbarriers: full[STAGES], empty[STAGES], cfull[2], cempty[2]
+    static constexpr size_t BAR = align16(CMETA + 2 * 16);
+    static constexpr size_t TOTAL = BAR + (2 * STAGES + 4) * 8;
 };
 
 struct TileArgs {
@@ -113,142 +121,122 @@ __device__ __forceinline__ double finish_row(double v, double alpha, double beta
     return fma(alpha, v, beta * __ldg(yp));              // general
 }
 
-// Stages tile `tile` into stage `s` (one producer thread): its owned-row
-// range (R0, R1) from the partition (passed in, prefetched by the caller),
-// val and col by bulk copy, and the row-pointer slice rowptr[R0 .. R1+1] by
-// bulk copy of its 16-byte-aligned superset (a few entries at the very end of
-// the array by plain loads).  All completes on the stage's mbarrier.
-template <int THREADS, int SIGMA, int VK>
-__device__ __forceinline__ void issue_tile(const TileArgs &a, unsigned char *smem, int tile,
-                                           int s, int R0, int R1, uint64_t pol)
+template <int SIGMA, int VK>
+struct Smem {
+    using L = Layout<SIGMA, VK>;
+    using VT = typename ValTraits<VK>::T;
+    unsigned char *base;
+    __device__ VT *val(int s) const { return reinterpret_cast<VT *>(base + L::VAL) + size_t(s) * L::TILE; }
+    __device__ int *col(int s) const { return reinterpret_cast<int *>(base + L::COL) + size_t(s) * L::TILE; }
+    __device__ int *rptr(int s) const { return reinterpret_cast<int *>(base + L::RPTR) + size_t(s) * L::RSLOT; }
+    __device__ int *meta(int s) const { return reinterpret_cast<int *>(base + L::META) + 4 * s; }
+    __device__ double *rval(int p) const { return reinterpret_cast<double *>(base + L::RVAL) + size_t(p) * L::RCAP; }
+    __device__ double *tailv(int p) const { return reinterpret_cast<double *>(base + L::TAILV) + p * TC; }
+    __device__ double *headv(int p) const { return reinterpret_cast<double *>(base + L::HEADV) + p * TC; }
+    __device__ double *cin() const { return reinterpret_cast<double *>(base + L::CIN); }
+    __device__ int *tailk(int p) const { return reinterpret_cast<int *>(base + L::TAILK) + p * TC; }
+    __device__ int *headk(int p) const { return reinterpret_cast<int *>(base + L::HEADK) + p * TC; }
+    __device__ int *cmeta(int p) const { return reinterpret_cast<int *>(base + L::CMETA) + 4 * p; }
+    __device__ uint64_t *bar() const { return reinterpret_cast<uint64_t *>(base + L::BAR); }
+    __device__ uint64_t *full(int s) const { return bar() + s; }
+    __device__ uint64_t *empty(int s) const { return bar() + STAGES + s; }
+    __device__ uint64_t *cfull(int p) const { return bar() + 2 * STAGES + p; }
+    __device__ uint64_t *cempty(int p) const { return bar() + 2 * STAGES + 2 + p; }
+};
+
+// Stages tile `tile` into stage `s` (the service warp, all lanes): owned-row
+// range (R0, R1), val and col by bulk copy, the row-pointer slice
+// rowptr[R0 .. R1+1] by bulk copy of its 16-byte-aligned superset; ragged
+// ends (and everything when a pointer is not 16-byte aligned) by plain loads
+// of the 32 lanes.  Completion: the stage's `full` mbarrier (one arrive with
+// the byte count, after the plain stores).
+template <int SIGMA, int VK>
+__device__ __forceinline__ void produce_tile(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+                                             int tile, int s, int R0, int R1, int lane,
+                                             uint64_t pol)
 {
-    using L = Layout<THREADS, SIGMA, VK>;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::BAR) + s;
-    int *meta = reinterpret_cast<int *>(smem + L::META) + 4 * s;
-    int *rslot = reinterpret_cast<int *>(smem + L::RPTR) + size_t(s) * L::RSLOT;
+    using L = Layout<SIGMA, VK>;
+    using VT = typename ValTraits<VK>::T;
     const long long tb = (long long)tile * L::TILE;
-    const long long cnt = (a.nnz - tb < L::TILE) ? (a.nnz - tb) : L::TILE;
-    uint32_t vbytes = 0, cbytes = 0, rbytes = 0;
-    if (a.use_tma) {
-        vbytes = (uint32_t)((cnt * L::VB) & ~15ll);
-        cbytes = (uint32_t)((cnt * 4) & ~15ll);
-    }
+    const int cnt = (int)((a.nnz - tb < L::TILE) ? (a.nnz - tb) : L::TILE);
+    const int vdone = a.use_tma ? (int)((((long long)cnt * L::VB) & ~15ll) / (L::VB ? L::VB : 1)) : 0;
+    const int cdone = a.use_tma ? (int)((((long long)cnt * 4) & ~15ll) / 4) : 0;
     const int nr = R1 - R0;
     const int fits = (nr + 2) <= L::RCAP;
-    int base = R0;
-    if (fits && a.rp_tma) {
+    int base = R0, t_end = R0, a1 = R0;
+    if (fits) {
         const int count = min(nr + 2, a.m - R0 + 1);   // rowptr[R0 .. R0+count-1]
-        const int a0 = R0 & ~3;
-        const int a1 = R0 + count;
-        const int safe_end = (a.m + 1) & ~3;            // bulk copies stay inside rowptr
-        const int t_end = max(a0, min((a1 + 3) & ~3, safe_end));
-        base = a0;
-        rbytes = (uint32_t)(t_end - a0) * 4u;
-        for (int i = t_end; i < a1; ++i) rslot[i - a0] = __ldg(a.rowptr + i);
+        a1 = R0 + count;
+        if (a.rp_tma) {
+            base = R0 & ~3;
+            const int safe_end = (a.m + 1) & ~3;        // bulk copies stay inside rowptr
+            t_end = max(base, min((a1 + 3) & ~3, safe_end));
+        }
     }
-    meta[0] = R0;
-    meta[1] = R1;
-    meta[2] = base;
-    meta[3] = fits;
-    ptx::mbar_arrive_expect_tx(bar, vbytes + cbytes + rbytes);   // release: meta, plain loads
-    if (vbytes)
-        ptx::bulk_g2s(smem + L::VAL + size_t(s) * L::TILE * L::VB,
-                      static_cast<const unsigned char *>(a.val) + tb * L::VB, vbytes, bar, pol);
-    if (cbytes)
-        ptx::bulk_g2s(smem + L::COL + size_t(s) * L::TILE * 4, a.col + tb, cbytes, bar, pol);
-    if (rbytes) ptx::bulk_g2s(rslot, a.rowptr + base, rbytes, bar, pol);
+    VT *vst = sm.val(s);
+    int *cst = sm.col(s);
+    int *rslot = sm.rptr(s);
+    if (VK != VAL_PATTERN)
+        for (int i = vdone + lane; i < cnt; i += 32) vst[i] = static_cast<const VT *>(a.val)[tb + i];
+    for (int i = cdone + lane; i < cnt; i += 32) cst[i] = __ldg(a.col + tb + i);
+    for (int i = t_end + lane; i < a1; i += 32) rslot[i - base] = __ldg(a.rowptr + i);
+    if (lane == 0) {
+        int *meta = sm.meta(s);
+        meta[0] = R0;
+        meta[1] = R1;
+        meta[2] = base;
+        meta[3] = fits;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const uint32_t vbytes = (uint32_t)vdone * L::VB;
+        const uint32_t cbytes = (uint32_t)cdone * 4u;
+        const uint32_t rbytes = (uint32_t)(t_end - base) * 4u;
+        ptx::mbar_arrive_expect_tx(sm.full(s), vbytes + cbytes + rbytes);  // release
+        if (vbytes)
+            ptx::bulk_g2s(vst, static_cast<const unsigned char *>(a.val) + tb * L::VB, vbytes,
+                          sm.full(s), pol);
+        if (cbytes) ptx::bulk_g2s(cst, a.col + tb, cbytes, sm.full(s), pol);
+        if (rbytes) ptx::bulk_g2s(rslot, a.rowptr + base, rbytes, sm.full(s), pol);
+    }
 }
 
-template <int THREADS, int SIGMA, int VK, int AB>
-__global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
+// Compute warp: for each tile of the CTA, one chunk of SIGMA consecutive
+// nonzeros per lane.  Row sums completed inside the chunk go to the carry
+// buffer of the tile's parity; the chunk's head (first segment of a row
+// begun earlier) and tail (partial of the row crossing the chunk end) are
+// published for the service warp.  No CTA-wide barrier.
+template <int SIGMA, int VK, int AB>
+__device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+                                             int cw, int lane, uint64_t pol_x)
 {
-    using L = Layout<THREADS, SIGMA, VK>;
+    using L = Layout<SIGMA, VK>;
     using VT = typename ValTraits<VK>::T;
     constexpr int TILE = L::TILE;
-    constexpr int PER = THREADS / 32;  // tails reduced per lane in the carry pass
-
-    extern __shared__ __align__(128) unsigned char smem[];
-    VT *val_s = reinterpret_cast<VT *>(smem + L::VAL);
-    int *col_s = reinterpret_cast<int *>(smem + L::COL);
-    int *rptr_base = reinterpret_cast<int *>(smem + L::RPTR);
-    const int *meta_s = reinterpret_cast<const int *>(smem + L::META);
-    double *rval_s = reinterpret_cast<double *>(smem + L::RVAL);
-    double *tailv_s = reinterpret_cast<double *>(smem + L::TAILV);
-    double *cin_s = reinterpret_cast<double *>(smem + L::CIN);
-    int *tailk_s = reinterpret_cast<int *>(smem + L::TAILK);
-    int *headk_s = reinterpret_cast<int *>(smem + L::HEADK);
-    double *headv_s = reinterpret_cast<double *>(smem + L::HEADV);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::BAR);
-
-    const int tid = threadIdx.x;
-    const int lane = tid & 31;
-    const int warp = tid >> 5;
-    const uint64_t pol_stream = ptx::policy_evict_first();
-    const uint64_t pol_x = ptx::policy_evict_last();
-
-    if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) ptx::mbar_init(bar + s, 1);
-        ptx::fence_mbar_init();
-    }
-    for (int i = tid; i < L::RCAP; i += THREADS) rval_s[i] = 0.0;  // kept zero between tiles
-    __syncthreads();
-    if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            const int t = blockIdx.x + s * gridDim.x;
-            if (t < a.ntiles)
-                issue_tile<THREADS, SIGMA, VK>(a, smem, t, s, __ldg(a.row_part + t),
-                                               __ldg(a.row_part + t + 1), pol_stream);
-        }
-    }
-
+    const int t = cw * 32 + lane;
     const double alpha = a.alpha, beta = a.beta;
-    int it = 0;
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x, ++it) {
-        const int s = it % STAGES;
-        const uint32_t parity = (uint32_t)((it / STAGES) & 1);
+    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+        const int s = i % STAGES;
+        const int p = i & 1;
+        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), WAIT_LIMIT_NS);
+        if (i >= 2)
+            ok = ok && ptx::mbar_wait_bounded(sm.cempty(p), (uint32_t)(((i - 2) / 2) & 1),
+                                              WAIT_LIMIT_NS);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            return;
+        }
+        const int *meta = sm.meta(s);
+        const int R0 = meta[0], R1 = meta[1], rbase = meta[2];
+        const bool fits = meta[3] != 0;
         const long long tb = (long long)tile * TILE;
         const int cnt_tile = (int)((a.nnz - tb < TILE) ? (a.nnz - tb) : TILE);
-        VT *vst = val_s + size_t(s) * TILE;
-        int *cst = col_s + size_t(s) * TILE;
-        int *rptr_s = rptr_base + size_t(s) * L::RSLOT;
-        // the producer prefetches the partition entries of the tile it will
-        // stage after this one's data is consumed
-        const int nt = tile + STAGES * (int)gridDim.x;
-        int nR0 = 0, nR1 = 0;
-        if (tid == 0 && nt < a.ntiles) {
-            nR0 = __ldg(a.row_part + nt);
-            nR1 = __ldg(a.row_part + nt + 1);
-        }
-        cin_s[tid] = 0.0;
-        if (tid == 0) a.carry[tile] = 0.0;
-        // ragged end of the tile (or everything, without TMA): plain loads
-        {
-            const int vdone = a.use_tma ? (int)(((long long)cnt_tile * L::VB & ~15ll) / (L::VB ? L::VB : 1)) : 0;
-            const int cdone = a.use_tma ? (int)(((long long)cnt_tile * 4 & ~15ll) / 4) : 0;
-            if (VK != VAL_PATTERN)
-                for (int i = vdone + tid; i < cnt_tile; i += THREADS)
-                    vst[i] = static_cast<const VT *>(a.val)[tb + i];
-            for (int i = cdone + tid; i < cnt_tile; i += THREADS) cst[i] = __ldg(a.col + tb + i);
-        }
-        const bool arrived = ptx::mbar_wait_bounded(bar + s, parity, WAIT_LIMIT_NS);
-        const int R0 = meta_s[4 * s + 0];
-        const int R1 = meta_s[4 * s + 1];
-        const int rbase = meta_s[4 * s + 2];
-        const bool fits = meta_s[4 * s + 3] != 0;     // CTA-uniform
-        const int nr = R1 - R0;                        // rows owned by this tile
-        if (arrived && fits && !a.rp_tma) {
-            const int nload = min(nr + 2, a.m - R0 + 1);
-            for (int i = tid; i < nload; i += THREADS) rptr_s[i] = __ldg(a.rowptr + R0 + i);
-        }
-        // B1: tile data and row pointer visible; a timed-out wait anywhere in
-        // the CTA stops the CTA (uniform decision)
-        if (__syncthreads_or(!arrived)) {
-            if (tid == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
-            break;
-        }
+        const VT *vst = sm.val(s);
+        const int *cst = sm.col(s);
+        const int *rptr_s = sm.rptr(s);
+        double *rval = sm.rval(p);
 
-        // ---------------- per-thread chunk: SIGMA consecutive nonzeros ----------
-        const int c0 = tid * SIGMA;                          // local offset in tile
+        const int c0 = t * SIGMA;                            // local offset in tile
         const int cnt = max(0, min(SIGMA, cnt_tile - c0));
         const int s0 = (int)(tb + c0);                       // global nnz index
         auto rp = [&](int r) -> int {                        // rowptr[r], r in [R0, R1+1]
@@ -296,12 +284,13 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
         double sum = 0.0;
         int head_row = -1;
         double head_val = 0.0;
+        double *headv = sm.headv(p);
         if (cnt > 0 && !warp_slow) {
             // branch-free FMA chain: at a row start the running sum is stored
             // (the first segment to the thread's head slot when the row began
             // in an earlier chunk) and restarted with a select
-            double *dst = sb ? &headv_s[tid] : &rval_s[r0 - R0];
-            double *nxt = &rval_s[r0 + 1 - R0];
+            double *dst = sb ? &headv[t] : &rval[r0 - R0];
+            double *nxt = &rval[r0 + 1 - R0];
 #pragma unroll
             for (int j = 0; j < SIGMA; ++j) {
                 const bool b = (mask >> j) & 1u;
@@ -314,10 +303,7 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
                     else sum = fma((double)vst[c0 + j], xv[j], sum);
                 }
             }
-            if (sb && mask != 0u) {
-                head_row = r0;
-                head_val = headv_s[tid];
-            }
+            if (sb && mask != 0u) head_row = r0;
         } else if (cnt > 0) {
             // general path: empty rows, or row pointer read from global memory
             int r = r0;
@@ -333,7 +319,7 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
                         head_row = r;
                         head_val = sum;
                     } else if (fits) {
-                        rval_s[r - R0] = sum;
+                        rval[r - R0] = sum;
                     } else {
                         a.y[r] = finish_row<AB>(sum, alpha, beta, a.y + r);
                     }
@@ -351,53 +337,122 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
                     else sum = fma((double)vst[c0 + j], xv[j], sum);
                 }
             }
+            headv[t] = head_val;
         }
-        tailv_s[tid] = sum;
-        tailk_s[tid] = (cnt > 0) ? rl : -1;   // -1: no data, never emitted
-        headk_s[tid] = head_row;
-        __syncthreads();  // B2: tails/heads published; stage s no longer read
+        sm.tailv(p)[t] = sum;
+        sm.tailk(p)[t] = (cnt > 0) ? rl : -1;   // -1: no data, never emitted
+        sm.headk(p)[t] = head_row;
+        if (t == 0) {
+            int *cm = sm.cmeta(p);
+            cm[0] = R0;
+            cm[1] = R1;
+            cm[2] = fits;
+            cm[3] = tile;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            ptx::mbar_arrive(sm.empty(s));   // stage s may be refilled
+            ptx::mbar_arrive(sm.cfull(p));   // carry buffers of this tile published
+        }
+    }
+}
 
-        if (tid == 0 && nt < a.ntiles) {
+// Service warp: stages tiles (producer) and, one tile behind the compute
+// warps, merges the chunk carries of each tile and writes its rows.
+//   carry pass: runs of equal rows among the TC tails are reduced lane-
+//   sequentially (NCW tails per lane, work-efficient), a 5-step segmented
+//   shuffle scan joins runs crossing lanes; each run total goes to the head
+//   of the chunk where the row ends, to a complete row, or to the tile carry;
+//   head pass: head + carry-in, one converged add per chunk;
+//   epilogue: alpha/beta once per row, coalesced stores of y.
+template <int SIGMA, int VK, int AB>
+__device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+                                             int lane, uint64_t pol_stream)
+{
+    using L = Layout<SIGMA, VK>;
+    constexpr int PER = NCW;  // tails reduced per lane
+    const double alpha = a.alpha, beta = a.beta;
+    int issued[STAGES];
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) issued[s] = 0;
+    for (int s = 0; s < STAGES; ++s) {
+        const int t = blockIdx.x + s * (int)gridDim.x;
+        if (t < a.ntiles) {
+            produce_tile<SIGMA, VK>(a, sm, t, s, __ldg(a.row_part + t), __ldg(a.row_part + t + 1),
+                                    lane, pol_stream);
+            ++issued[s];
+        }
+    }
+    double *cin = sm.cin();
+    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+        const int s = i % STAGES;
+        const int p = i & 1;
+        // partition entries of the tile this stage is refilled with
+        const int nt = tile + STAGES * (int)gridDim.x;
+        int nR0 = 0, nR1 = 0;
+        if (nt < a.ntiles) {
+            nR0 = __ldg(a.row_part + nt);
+            nR1 = __ldg(a.row_part + nt + 1);
+        }
+        bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1), WAIT_LIMIT_NS);
+        if (ok && nt < a.ntiles)
+            ok = ptx::mbar_wait_bounded(sm.empty(s), (uint32_t)((i / STAGES) & 1), WAIT_LIMIT_NS);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            break;
+        }
+        if (nt < a.ntiles) {
             ptx::fence_proxy_async_smem();
-            issue_tile<THREADS, SIGMA, VK>(a, smem, nt, s, nR0, nR1, pol_stream);
+            produce_tile<SIGMA, VK>(a, sm, nt, s, nR0, nR1, lane, pol_stream);
+            ++issued[s];
         }
+        const int *cm = sm.cmeta(p);
+        const int R0 = cm[0], R1 = cm[1];
+        const bool fits = cm[2] != 0;
+        double *rval = sm.rval(p);
+        const double *tailv = sm.tailv(p);
+        const int *tailk = sm.tailk(p);
+        const int *headk = sm.headk(p);
+        const double *headv = sm.headv(p);
 
-        // ---------------- carry pass: reduce runs of tails (warp 0) ------------
-        if (warp == 0) {
+        // ---------------- carry pass -------------------------------------
+        {
             auto emit = [&](int key, double total, int after) {
                 if (key < 0) return;
-                if (after < THREADS && headk_s[after] == key) {
-                    cin_s[after] = total;                    // joins a head
-                } else if (after >= THREADS && key == R1) {
+                if (after < TC && headk[after] == key) {
+                    cin[after] = total;                      // joins a head
+                } else if (after >= TC && key == R1) {
                     a.carry[tile] = total;                   // continues in next tile
                 } else if (fits) {
-                    rval_s[key - R0] = total;                // complete row
+                    rval[key - R0] = total;                  // complete row
                 } else {
                     a.y[key] = finish_row<AB>(total, alpha, beta, a.y + key);
                 }
             };
+            if (lane == 0) a.carry[tile] = 0.0;
+            __syncwarp();
             const int base = lane * PER;
             double acc = 0.0;
-            int prevk = tailk_s[base];
+            int prevk = tailk[base];
             const int fk = prevk;
             double af = 0.0;
             int f_after = base + PER;
             bool broke = false;
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
-                const int i = base + q;
-                const int key = tailk_s[i];
+                const int ii = base + q;
+                const int key = tailk[ii];
                 const bool brk = (q > 0) && (key != prevk);
                 if (brk) {
                     if (!broke) {
                         af = acc;
-                        f_after = i;
+                        f_after = ii;
                         broke = true;
                     } else {
-                        emit(prevk, acc, i);
+                        emit(prevk, acc, ii);
                     }
                 }
-                acc = (brk ? 0.0 : acc) + tailv_s[i];
+                acc = (brk ? 0.0 : acc) + tailv[ii];
                 prevk = key;
             }
             const bool single = !broke;
@@ -405,59 +460,90 @@ __global__ void __launch_bounds__(THREADS) tile_spmv_kernel(const TileArgs a)
             double S = acc;
             const int kl_prev = __shfl_up_sync(0xffffffffu, kl, 1);
             bool f = (lane == 0) || !single || (kl != kl_prev);
+            // segmented scan across lanes, only where a lane's last run
+            // continues from its left neighbour somewhere in the warp
+            if (__any_sync(0xffffffffu, !f)) {
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const double So = __shfl_up_sync(0xffffffffu, S, d);
-                const bool fo = __shfl_up_sync(0xffffffffu, f, d);
-                const bool take = (lane >= d) && !f;
-                S = S + (take ? So : 0.0);
-                f = take ? fo : f;
+                for (int d = 1; d < 32; d <<= 1) {
+                    const double So = __shfl_up_sync(0xffffffffu, S, d);
+                    const bool fo = __shfl_up_sync(0xffffffffu, f, d);
+                    const bool take = (lane >= d) && !f;
+                    S = S + (take ? So : 0.0);
+                    f = take ? fo : f;
+                }
             }
             const double S_prev = __shfl_up_sync(0xffffffffu, S, 1);
             // first run of a lane with several runs may continue from the left
             const double tot = af + ((lane > 0 && kl_prev == fk) ? S_prev : 0.0);
             if (!single) emit(fk, tot, f_after);
             // last run ends here unless the next lane starts with the same row
-            const int next_first = (lane < 31) ? tailk_s[base + PER] : INT_MIN;
+            const int next_first = (lane < 31) ? tailk[base + PER] : INT_MIN;
             if (lane == 31 || next_first != kl) emit(kl, S, base + PER);
         }
-        __syncthreads();  // B3: carries in
-
-        {   // head pass: every thread adds its carry-in once (converged add)
-            const double hv = head_val + cin_s[tid];
-            if (head_row >= 0) {
-                if (fits) rval_s[head_row - R0] = hv;
-                else a.y[head_row] = finish_row<AB>(hv, alpha, beta, a.y + head_row);
+        __syncwarp();
+        // ---------------- head pass: one converged add per chunk ----------
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int tt = q * 32 + lane;
+            const int hr = headk[tt];
+            const double hv = headv[tt] + cin[tt];
+            cin[tt] = 0.0;
+            if (hr >= 0) {
+                if (fits) rval[hr - R0] = hv;
+                else a.y[hr] = finish_row<AB>(hv, alpha, beta, a.y + hr);
             }
         }
-        __syncthreads();  // B4: row sums final
-
+        __syncwarp();
+        // ---------------- epilogue: finished rows out, slots cleared ------
+        const int nr = R1 - R0;
         if (fits) {
-            // finished rows out (coalesced); the row-sum slots are cleared for
-            // the next tile, which writes them only after its B1
-            for (int i = tid; i < nr; i += THREADS) {
-                a.y[R0 + i] = finish_row<AB>(rval_s[i], alpha, beta, a.y + R0 + i);
-                rval_s[i] = 0.0;
+            for (int r = lane; r < nr; r += 32) {
+                a.y[R0 + r] = finish_row<AB>(rval[r], alpha, beta, a.y + R0 + r);
+                rval[r] = 0.0;
             }
         } else {
-            // rows without nonzeros were skipped above; write them here
-            for (int rr = R0 + tid; rr < R1; rr += THREADS)
+            for (int rr = R0 + lane; rr < R1; rr += 32)
                 if (__ldg(a.rowptr + rr) == __ldg(a.rowptr + rr + 1))
                     a.y[rr] = finish_row<AB>(0.0, alpha, beta, a.y + rr);
         }
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(sm.cempty(p));
     }
+    // drain: copies issued into a stage and never consumed (early exit only)
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; ++s)
+            if (issued[s] > 0)
+                ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((issued[s] - 1) & 1), WAIT_LIMIT_NS);
+    }
+}
 
-    // drain: a tile whose copies were issued but not consumed (early exit)
+template <int SIGMA, int VK, int AB>
+__global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a)
+{
+    using L = Layout<SIGMA, VK>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const Smem<SIGMA, VK> sm{smem_raw};
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
     if (tid == 0) {
-        for (int k = 0; k < STAGES; ++k) {
-            const int t = blockIdx.x + (it + k) * (int)gridDim.x;
-            if (t < a.ntiles) {
-                const int s = (it + k) % STAGES;
-                ptx::mbar_wait_bounded(bar + s, (uint32_t)(((it + k) / STAGES) & 1),
-                                       WAIT_LIMIT_NS);
-            }
+        for (int s = 0; s < STAGES; ++s) {
+            ptx::mbar_init(sm.full(s), 1);
+            ptx::mbar_init(sm.empty(s), NCW);
         }
+        for (int p = 0; p < 2; ++p) {
+            ptx::mbar_init(sm.cfull(p), NCW);
+            ptx::mbar_init(sm.cempty(p), 1);
+        }
+        ptx::fence_mbar_init();
     }
+    for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
+    for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
+    __syncthreads();
+    if (warp == NCW)
+        service_warp<SIGMA, VK, AB>(a, sm, lane, ptx::policy_evict_first());
+    else
+        compute_warp<SIGMA, VK, AB>(a, sm, warp, lane, ptx::policy_evict_last());
 }
 
 // part[k] = number of rows r with rowptr[r+1] <= k*TILE (k = 1..ntiles-1);
@@ -508,15 +594,14 @@ __global__ void scale_y_kernel(int m, double beta, double *__restrict__ y)
 }
 
 // ---------------- compiled shapes -----------------------------------------
-constexpr int kThreads = 128;
-constexpr int kSigmas[] = {7, 11, 15, 19, 23};
+constexpr int kSigmas[] = {11, 15, 19, 23, 27};
 constexpr int kNumSigmas = sizeof(kSigmas) / sizeof(kSigmas[0]);
 
 template <int SIGMA, int VK, int AB>
 int launch_shape(const TileArgs &a, cudaStream_t stream)
 {
-    using L = Layout<kThreads, SIGMA, VK>;
-    auto kfn = tile_spmv_kernel<kThreads, SIGMA, VK, AB>;
+    using L = Layout<SIGMA, VK>;
+    auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
     static int configured_dev = -1;
     static int blocks_per_sm = 0;
     int dev = 0;
@@ -525,7 +610,7 @@ int launch_shape(const TileArgs &a, cudaStream_t stream)
         SBLAS_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)L::TOTAL));
         int bps = 0;
-        SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, kThreads,
+        SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA_THREADS,
                                                                      L::TOTAL));
         if (bps < 1) {
             set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
@@ -536,7 +621,7 @@ int launch_shape(const TileArgs &a, cudaStream_t stream)
         configured_dev = dev;
     }
     const int grid = min(a.ntiles, blocks_per_sm * device_num_sms());
-    kfn<<<grid, kThreads, L::TOTAL, stream>>>(a);
+    kfn<<<grid, CTA_THREADS, L::TOTAL, stream>>>(a);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }
@@ -565,7 +650,7 @@ int launch_vk(int vk, const TileArgs &a, cudaStream_t stream)
 }  // namespace
 
 int tile_shape_count() { return kNumSigmas; }
-TileShape tile_shape_at(int i) { return TileShape{kThreads, kSigmas[i]}; }
+TileShape tile_shape_at(int i) { return TileShape{TC, kSigmas[i]}; }
 int tile_shape_index(int sigma)
 {
     for (int i = 0; i < kNumSigmas; ++i)
@@ -577,7 +662,7 @@ static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 size_t tile_workspace_bytes(long long nnz, int sigma)
 {
-    const long long tile = (long long)kThreads * sigma;
+    const long long tile = (long long)TC * sigma;
     const long long ntiles = (nnz + tile - 1) / tile;
     return align256(sizeof(int) * (size_t)(ntiles + 1)) + align256(sizeof(double) * (size_t)ntiles) +
            256;
@@ -587,7 +672,7 @@ int default_sigma_for(int m, long long nnz)
 {
     (void)m;
     (void)nnz;
-    return 19;
+    return 23;
 }
 
 int csr5_sigma_for(int m, long long nnz)
@@ -626,7 +711,7 @@ int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void
         set_error(SBLAS_ERR_UNSUPPORTED, "sigma %d is not a compiled tile shape", sigma);
         return SBLAS_ERR_UNSUPPORTED;
     }
-    const long long tile = (long long)kThreads * sigma;
+    const long long tile = (long long)TC * sigma;
     const long long ntiles_ll = (nnz + tile - 1) / tile;
     if (ntiles_ll > INT_MAX - 2) {
         set_error(SBLAS_ERR_ARG, "nnz %lld too large", nnz);
@@ -651,7 +736,7 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
         set_error(SBLAS_ERR_UNSUPPORTED, "sigma %d is not a compiled tile shape", sigma);
         return SBLAS_ERR_UNSUPPORTED;
     }
-    const long long tile = (long long)kThreads * sigma;
+    const long long tile = (long long)TC * sigma;
     const long long ntiles_ll = (nnz + tile - 1) / tile;
     if (ntiles_ll > INT_MAX - 2) {
         set_error(SBLAS_ERR_ARG, "nnz %lld too large", nnz);
@@ -688,11 +773,11 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     a.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
     int rc = SBLAS_OK;
     switch (sigma) {
-    case 7: rc = launch_vk<7>(val_kind, a, stream); break;
     case 11: rc = launch_vk<11>(val_kind, a, stream); break;
     case 15: rc = launch_vk<15>(val_kind, a, stream); break;
     case 19: rc = launch_vk<19>(val_kind, a, stream); break;
     case 23: rc = launch_vk<23>(val_kind, a, stream); break;
+    case 27: rc = launch_vk<27>(val_kind, a, stream); break;
     default: rc = SBLAS_ERR_UNSUPPORTED; break;
     }
     if (rc != SBLAS_OK) return rc;
