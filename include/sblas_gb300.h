@@ -108,6 +108,23 @@ SBLAS_API int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, dou
                                     const int *col, const double *x, double beta, double *y,
                                     int sigma, void *work, size_t work_bytes, void *stream);
 
+/* Allocation-free FP64 CSR SpMV (the tile kernel, default tile shape) for
+ * callers that cannot call cudaMalloc when they need it: code running inside
+ * a device-memory pool or caching allocator, or services that reserve all
+ * device memory at start-up and forbid allocation afterwards.  This entry
+ * point has no counterpart in the reference.
+ * Scratch: a fixed file-scope device array of sblas_noalloc_scratch_bytes()
+ * bytes (4 MiB, held by every GPU that loads the library until exit); larger
+ * matrices (about 0.8 G nonzeros and up) fail with SBLAS_ERR_ARG.  The
+ * array is shared by every call: calls that overlap on the GPU race.  The
+ * first call on a device resolves the array's address and creates the
+ * library's per-device context (no device memory): make it before any
+ * stream capture.  Device arrays, stream-ordered on `stream`. */
+SBLAS_API size_t sblas_noalloc_scratch_bytes(void);
+SBLAS_API int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const double *val,
+                                   const int *rowptr, const int *col, const double *x,
+                                   double beta, double *y, void *stream);
+
 /* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
  * then runs the tile kernel.  rowptr_work: int[m + 1] device buffer. */
 SBLAS_API int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
