@@ -364,8 +364,12 @@ __device__ __forceinline__ bool finish_chunk(const TileArgs &a, const Smem<SIGMA
         }
         headv[t] = head_val;
     }
-    sm.tailv(p)[t] = sum;
-    sm.tailk(p)[t] = (cnt > 0) ? c.rl : -1;   // -1: no data, never emitted
+    // tails stored transposed (thread t at (t % NCW) * 32 + t / NCW) so that
+    // the carry pass, where lane l reads threads l*NCW .. l*NCW+NCW-1, is
+    // free of shared-memory bank conflicts
+    const int tslot = (t % NCW) * 32 + t / NCW;
+    sm.tailv(p)[tslot] = sum;
+    sm.tailk(p)[tslot] = (cnt > 0) ? c.rl : -1;   // -1: no data, never emitted
     sm.headk(p)[t] = head_row;
     if (t == 0) {
         int *cm = sm.cmeta(p);
@@ -440,15 +444,25 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
         }
     }
     double *cin = sm.cin();
+    // partition entries of the tile staged at iteration i (tile + STAGES*G),
+    // loaded one iteration ahead so their DRAM latency stays hidden
+    int nR0 = 0, nR1 = 0;
+    {
+        const int nt0 = blockIdx.x + STAGES * (int)gridDim.x;
+        if (nt0 < a.ntiles) {
+            nR0 = __ldg(a.row_part + nt0);
+            nR1 = __ldg(a.row_part + nt0 + 1);
+        }
+    }
     for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
         const int s = i % STAGES;
         const int p = i & 1;
-        // partition entries of the tile this stage is refilled with
         const int nt = tile + STAGES * (int)gridDim.x;
-        int nR0 = 0, nR1 = 0;
-        if (nt < a.ntiles) {
-            nR0 = __ldg(a.row_part + nt);
-            nR1 = __ldg(a.row_part + nt + 1);
+        const int nt2 = nt + (int)gridDim.x;
+        int fR0 = 0, fR1 = 0;
+        if (nt2 < a.ntiles) {
+            fR0 = __ldg(a.row_part + nt2);
+            fR1 = __ldg(a.row_part + nt2 + 1);
         }
         bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1), WAIT_LIMIT_NS);
         if (ok && nt < a.ntiles)
@@ -462,6 +476,8 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
             produce_tile<SIGMA, VK>(a, sm, nt, s, nR0, nR1, lane, pol_stream);
             ++issued[s];
         }
+        nR0 = fR0;
+        nR1 = fR1;
         const int *cm = sm.cmeta(p);
         const int R0 = cm[0], R1 = cm[1];
         const bool fits = cm[2] != 0;
@@ -487,17 +503,17 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
             };
             if (lane == 0) a.carry[tile] = 0.0;
             __syncwarp();
-            const int base = lane * PER;
+            const int base = lane * PER;          // first thread of this lane's tails
             double acc = 0.0;
-            int prevk = tailk[base];
+            int prevk = tailk[lane];              // thread base at slot 0*32 + lane
             const int fk = prevk;
             double af = 0.0;
             int f_after = base + PER;
             bool broke = false;
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
-                const int ii = base + q;
-                const int key = tailk[ii];
+                const int ii = base + q;          // thread index (heads use it)
+                const int key = tailk[q * 32 + lane];
                 const bool brk = (q > 0) && (key != prevk);
                 if (brk) {
                     if (!broke) {
@@ -508,7 +524,7 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
                         emit(prevk, acc, ii);
                     }
                 }
-                acc = (brk ? 0.0 : acc) + tailv[ii];
+                acc = (brk ? 0.0 : acc) + tailv[q * 32 + lane];
                 prevk = key;
             }
             const bool single = !broke;
@@ -533,7 +549,7 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
             const double tot = af + ((lane > 0 && kl_prev == fk) ? S_prev : 0.0);
             if (!single) emit(fk, tot, f_after);
             // last run ends here unless the next lane starts with the same row
-            const int next_first = (lane < 31) ? tailk[base + PER] : INT_MIN;
+            const int next_first = (lane < 31) ? tailk[lane + 1] : INT_MIN;
             if (lane == 31 || next_first != kl) emit(kl, S, base + PER);
         }
         __syncwarp();
