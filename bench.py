@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--m", type=int, default=4_000_000,
                    help="rows of the power-law matrix (smaller only for profiling captures)")
     p.add_argument("--sigma", type=int, default=0, help="tile shape (0 = library default)")
+    p.add_argument("--probe", action="store_true",
+                   help="print the hardware ceilings (FP64 pipe, random gathers, HBM read)")
     p.add_argument("--kernel-only", action="store_true",
                    help="time the device steps only (no e2e, CPU baseline, extras): the "
                         "small case used for ncu captures")
@@ -417,8 +419,31 @@ def run_extras(dev, stream, args):
     return res
 
 
+def run_probe():
+    """The ceilings that bound FP64 SpMV on this GPU (library probes)."""
+    import ctypes as C
+    import torch
+    from hpda_sblas_pnnl_gb300 import _lib
+    torch.cuda.init()
+    lib = _lib.load(build_if_missing=True)
+    full, one, gps, bps = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    _lib.check(lib.sblas_probe_fp64(C.byref(full), C.byref(one)))
+    out = {"fp64_dfma_warp_instr_per_s_32_lanes": full.value,
+           "fp64_dfma_warp_instr_per_s_1_lane": one.value,
+           "fp64_dfma_lane_ops_per_s": 32 * full.value}
+    for rng in (4_000_000, 250_000, 16_384):
+        _lib.check(lib.sblas_probe_gather(rng, C.byref(gps)))
+        out[f"random_8B_gathers_per_s_range_{rng}"] = gps.value
+    _lib.check(lib.sblas_probe_stream(C.byref(bps)))
+    out["hbm_read_bytes_per_s"] = bps.value
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.probe:
+        run_probe()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -125,6 +125,14 @@ SBLAS_API int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const do
                                    const int *rowptr, const int *col, const double *x,
                                    double beta, double *y, void *stream);
 
+/* Hardware probes (diagnostics; allocate their own buffers and synchronise):
+ * FP64 DFMA warp instructions per second with 32 and with 1 active lane;
+ * random 8-byte gathers per second from a vector of `range` doubles;
+ * streaming HBM read bytes per second. */
+SBLAS_API int sblas_probe_fp64(double *warp_instr_per_s_full, double *warp_instr_per_s_one_lane);
+SBLAS_API int sblas_probe_gather(int range, double *gathers_per_s);
+SBLAS_API int sblas_probe_stream(double *bytes_per_s);
+
 /* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
  * then runs the tile kernel.  rowptr_work: int[m + 1] device buffer. */
 SBLAS_API int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
