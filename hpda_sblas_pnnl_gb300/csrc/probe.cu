@@ -68,9 +68,19 @@ __global__ void probe_gather_kernel(const double *__restrict__ x, const int *__r
 
 __global__ void probe_stream_kernel(const double2 *__restrict__ p, size_t n2, double *out)
 {
+    // four independent 16-byte loads in flight per thread per iteration
+    constexpr int U = 4;
     double acc = 0.0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < n2; i += U * stride) {
+        double2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = __ldcs(p + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc += v[u].x + v[u].y;
+    }
+    for (; i < n2; i += stride) {
         const double2 v = __ldcs(p + i);
         acc += v.x + v.y;
     }

@@ -229,3 +229,52 @@ def test_csr5_kernel_device_entry(sblas_lib, cuda):
     assert rc == 0
     torch.cuda.synchronize()
     assert_close(y.cpu().numpy(), g["y_ref_csr"])
+
+
+# ---- mixed-precision forms: FP32-stored values, pattern-only ---------------
+
+@pytest.mark.parametrize("name", ["zipf200_ab", "long_row", "empty_rows", "sparse_rows",
+                                  "diag3000", "g200", "one"])
+def test_fp32_values_and_pattern_forms(sblas_lib, cuda, name):
+    """FP32-stored values (products and chunk sums in double-float, row sums
+    in FP64): within 1e-12 of the FP64 result on the FP32-rounded values, and
+    within 1e-6 of the FP64 oracle.  Pattern-only: every stored entry is 1."""
+    from hpda_sblas_pnnl_gb300 import ops
+    g = load_golden(name)
+    m, n = int(g["m"]), int(g["n"])
+    a, b = float(g["alpha"]), float(g["beta"])
+    v32 = g["val"].astype(np.float32)
+    ref32 = O.csr_spmv(m, n, g["rowptr"], g["col"], v32.astype(np.float64), g["x"], g["y0"], a, b)
+    refpat = O.csr_spmv(m, n, g["rowptr"], g["col"], np.ones_like(g["val"]), g["x"], g["y0"], a, b)
+    for s in sigmas():
+        rp, c, _, x, y = dev(g, cuda)
+        v = torch.from_numpy(v32).to(cuda)
+        ops.csrmv(rp, c, v, x, y, a, b, n=n, sigma=s)
+        torch.cuda.synchronize()
+        assert_close(y.cpu().numpy(), ref32)
+        assert rel_l2(y.cpu().numpy(), g["y_ref_csr"]) <= 1e-6
+        rp, c, _, x, y = dev(g, cuda)
+        ops.csrmv(rp, c, None, x, y, a, b, n=n, sigma=s)
+        torch.cuda.synchronize()
+        assert_close(y.cpu().numpy(), refpat)
+
+
+def test_double_float_forms_fall_back_on_extreme_values(sblas_lib, cuda):
+    """Operands outside the double-float range (|x| >= 2^61, tiny values,
+    huge FP32 values) take FP64 arithmetic: results stay FP64-accurate."""
+    from hpda_sblas_pnnl_gb300 import ops, synth
+    a, x = synth.powerlaw(m=20_000, mean_deg=17.5, seed=3, device=cuda, values="normal")
+    x = x.clone()
+    x[::97] = 1e300
+    x[5::89] = 1e-200
+    v32 = a.val.to(torch.float32)
+    v32[::1013] = 3e37
+    ref = O.csr_spmv(a.m, a.n, a.rowptr.cpu().numpy(), a.col.cpu().numpy(),
+                     v32.double().cpu().numpy(), x.cpu().numpy(), np.zeros(a.m))
+    y = torch.zeros(a.m, dtype=torch.float64, device=cuda)
+    ops.csrmv(a.rowptr, a.col, v32, x, y)
+    torch.cuda.synchronize()
+    yy = y.cpu().numpy()
+    assert np.isfinite(yy).all() == np.isfinite(ref).all()
+    fin = np.isfinite(ref)
+    assert rel_l2(yy[fin], ref[fin]) <= 1e-12
