@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-extras", action="store_true", help="skip the other forms")
+    p.add_argument("--forms", default="banded,pattern,coo,batch,autograd",
+                   help="comma list of the other forms to measure")
     p.add_argument("--seed", type=int, default=2021)
     p.add_argument("--m", type=int, default=4_000_000,
                    help="rows of the power-law matrix (smaller only for profiling captures)")
@@ -355,9 +357,10 @@ def run_ours(args):
 
 
 def run_extras(dev, stream, args):
-    """The other forms, each timed with CUDA events (kernel time, analysed
-    plan): banded FP64 and FP32-values, pattern-only power-law.  Errors are
-    relative L2 against the FP64 oracle's result on the same inputs."""
+    """The other forms, each timed with CUDA events (analysed plans): banded
+    FP64 and FP32 values, pattern-only and COO power-law (errors: relative
+    L2 against the FP64 oracle on the same inputs), the batched uneven SpMM
+    and the differentiable SpMM (see their functions)."""
     import numpy as np
     import torch
     from hpda_sblas_pnnl_gb300 import ops, synth
@@ -371,6 +374,26 @@ def run_extras(dev, stream, args):
             plan(x, y)
         return statistics.mean(cuda_event_ms(lambda: plan(x, y), stream, reps))
 
+    forms = set(args.forms.split(","))
+    if "banded" in forms:
+        res.update(run_banded_extra(dev, stream, args, timed, threads, pk))
+    if "pattern" in forms or "coo" in forms:
+        res.update(run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms))
+    if "batch" in forms:
+        res["batched"] = run_batch_extra(dev, stream, args)
+        torch.cuda.empty_cache()
+    if "autograd" in forms:
+        res["autograd"] = run_autograd_extra(dev, stream, args)
+        torch.cuda.empty_cache()
+    return res
+
+
+def run_banded_extra(dev, stream, args, timed, threads, pk):
+    import numpy as np
+    import torch
+    from hpda_sblas_pnnl_gb300 import ops, synth
+    from oracle import oracle as O
+    res = {}
     a, x = synth.banded_fem(device=dev)
     m, n, nnz = a.m, a.n, a.nnz
     rp, c, v = a.numpy()
@@ -389,7 +412,15 @@ def run_extras(dev, stream, args):
         res["fp32val_speedup"] = round(res["banded_fp64"]["us"] / res["banded_fp32val"]["us"], 3)
     del a, x, y
     torch.cuda.empty_cache()
+    return res
 
+
+def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
+    import numpy as np
+    import torch
+    from hpda_sblas_pnnl_gb300 import ops, synth
+    from oracle import oracle as O
+    res = {}
     a, x = synth.powerlaw(seed=args.seed, device=dev)
     y = torch.zeros(a.m, dtype=torch.float64, device=dev)
     plan = ops.CsrPlan(a.rowptr, a.col, None)
@@ -416,6 +447,127 @@ def run_extras(dev, stream, args):
                            "frac": round(bcoo / coo_ms / 1e6 / pk, 4), "us": round(coo_ms * 1e3, 1),
                            "note": "row pointer built on device each call, then tile kernel"}
     res["powerlaw_csc_to_csr_ms"] = round(conv_ms, 2)
+    del a, x, y
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_batch_extra(dev, stream, args):
+    """Batched uneven SpMM: 64 matrices (rows log-uniform in [10k, 1M], mean
+    nonzeros per row log-uniform in [4, 64], half power-law, half banded),
+    k in {1, 4, 8} right-hand sides ~ U(-1, 1).  One graph-captured run of
+    the batched plan (s picked by the autotuner) against 64 * k launches of
+    the single-matrix tile kernel (one per matrix and right-hand side,
+    analysed plans, eager), both timed with CUDA events; agreement of the two
+    results (relative L2) is the correctness check at this size."""
+    import numpy as np
+    import torch
+    from hpda_sblas_pnnl_gb300 import ops, synth, tune
+    pk, _ = peaks()
+    mats = synth.batch_uneven(nmat=64, seed=args.seed + 64, device=dev)
+    total_nnz = sum(a.nnz for a in mats)
+    res = {"matrices": len(mats), "nnz": total_nnz,
+           "rows": [min(a.m for a in mats), max(a.m for a in mats)]}
+    single = [ops.CsrPlan(a.rowptr, a.col, a.val) for a in mats]
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 7)
+    for k in (1, 4, 8):
+        xs = [(torch.rand((a.n, k), generator=g, dtype=torch.float64, device=dev) * 2 - 1)
+              for a in mats]
+        if k == 1:
+            xs = [x.view(-1) for x in xs]
+        ys = [torch.zeros((a.m, k) if k > 1 else (a.m,), dtype=torch.float64, device=dev)
+              for a in mats]
+        trip = [(a.rowptr, a.col, a.val) for a in mats]
+        s_best, s_times = tune.batch_s(trip, xs, k)
+        plan = ops.BatchPlan(trip, xs, ys, k, s=s_best)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            plan()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            plan()
+        for _ in range(3):
+            graph.replay()
+        b_ms = statistics.median(cuda_event_ms(graph.replay, stream, 10))
+        # per-matrix, per-column launches of the single-matrix kernel
+        xc = [[x.view(x.shape[0], -1)[:, c].contiguous() for c in range(k)] for x in xs]
+        yc = [[torch.zeros(a.m, dtype=torch.float64, device=dev) for _ in range(k)] for a in mats]
+
+        def per_matrix():
+            for p, xcs, ycs in zip(single, xc, yc):
+                for c in range(k):
+                    p(xcs[c], ycs[c])
+
+        per_matrix()
+        p_ms = statistics.median(cuda_event_ms(per_matrix, stream, 5))
+        num = den = 0.0
+        for y, ycs in zip(ys, yc):
+            yy = y.view(y.shape[0], -1)
+            for c in range(k):
+                num += float(((yy[:, c] - ycs[c]) ** 2).sum())
+                den += float((ycs[c] ** 2).sum())
+        bytes_k = sum(synth.compulsory_bytes(a.m, a.n, a.nnz, k=k) for a in mats)
+        flops = 2.0 * total_nnz * k
+        res[f"k{k}"] = {
+            "batched_ms": round(b_ms, 3), "per_matrix_ms": round(p_ms, 3),
+            "speedup_vs_per_matrix": round(p_ms / b_ms, 3),
+            "gbs": round(bytes_k / b_ms / 1e6, 1), "frac_hbm": round(bytes_k / b_ms / 1e6 / pk, 4),
+            "fp64_tflops": round(flops / b_ms / 1e9, 4), "s": s_best,
+            "tuner_ms": {str(sv): round(t, 3) for sv, t in s_times.items()},
+            "units": plan.units, "launches": "1 graph (batched kernel + carry fix-up)",
+            "per_matrix_launches": 64 * k * 2, "rel_l2_vs_per_matrix": (num / den) ** 0.5,
+        }
+        plan.close()
+        del graph, xs, ys, xc, yc
+        torch.cuda.empty_cache()
+    return res
+
+
+def run_autograd_extra(dev, stream, args):
+    """Differentiable SpMM: 1.0M-row power-law CSR, ~20M nonzeros, values
+    N(0, 1), X (n x 16) and upstream G (m x 16) N(0, 1).  forward = Y = A X;
+    forward + backward = the same through autograd.spmm plus backward(G)
+    (dX = A^T G and dval), measured with CUDA events, FP64 and FP32 values."""
+    import torch
+    from hpda_sblas_pnnl_gb300 import autograd, synth
+    a, _ = synth.powerlaw(m=1_000_000, mean_deg=20.0, seed=args.seed + 5, device=dev,
+                          values="normal")
+    k = 16
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 9)
+    x0 = torch.randn((a.n, k), generator=g, dtype=torch.float64, device=dev)
+    gy = torch.randn((a.m, k), generator=g, dtype=torch.float64, device=dev)
+    res = {"m": a.m, "nnz": a.nnz, "k": k}
+    for name, dtype in (("fp64", torch.float64), ("fp32val", torch.float32)):
+        op = autograd.CsrOperator(a.rowptr, a.col, a.n, k, value_dtype=dtype)
+        val = a.val.to(dtype).requires_grad_(True)
+        x = x0.clone().requires_grad_(True)
+        y = torch.empty((a.m, k), dtype=torch.float64, device=dev)
+
+        def fwd():
+            op.fwd(x.detach(), y, val=val.detach())
+
+        def fwd_bwd():
+            val.grad = None
+            x.grad = None
+            autograd.spmm(op, val, x).backward(gy)
+
+        for _ in range(3):
+            fwd()
+            fwd_bwd()
+        f_ms = statistics.median(cuda_event_ms(fwd, stream, 10))
+        fb_ms = statistics.median(cuda_event_ms(fwd_bwd, stream, 10))
+        vb = 8 if dtype == torch.float64 else 4
+        fbytes = synth.compulsory_bytes(a.m, a.n, a.nnz, val_bytes=vb, k=k)
+        res[name] = {"fwd_ms": round(f_ms, 3), "fwd_bwd_ms": round(fb_ms, 3),
+                     "ratio": round(fb_ms / f_ms, 3),
+                     "fwd_fp64_tflops": round(2.0 * a.nnz * k / f_ms / 1e9, 4),
+                     "fwd_gbs": round(fbytes / f_ms / 1e6, 1)}
+        del op, val, x, y
+        torch.cuda.empty_cache()
     return res
 
 

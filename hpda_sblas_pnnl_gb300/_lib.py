@@ -32,6 +32,25 @@ class SpmvRet(C.Structure):
         return self.comp_time < 0
 
 
+class BatchMatrix(C.Structure):
+    """include/sblas_gb300.h (sblas_batch_matrix): one matrix of a batch."""
+
+    _fields_ = [
+        ("m", C.c_int),
+        ("n", C.c_int),
+        ("nnz", C.c_longlong),
+        ("val", C.c_void_p),
+        ("rowptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("x", C.c_void_p),
+        ("ldx", C.c_int),
+        ("y", C.c_void_p),
+        ("ldy", C.c_int),
+        ("alpha", C.c_double),
+        ("beta", C.c_double),
+    ]
+
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
@@ -68,6 +87,20 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_csc_to_csr": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp,
                                    _vp, C.c_size_t, _vp]),
     "sblas_coo_rows_to_rowptr": (C.c_int, [C.c_int, C.c_longlong, _vp, _vp, _vp]),
+    "sblas_batch_default_s": (C.c_int, [C.c_int]),
+    "sblas_batch_plan_create": (C.c_int, [C.c_int, C.POINTER(BatchMatrix), C.c_int, C.c_int,
+                                          C.c_int, _vp, C.POINTER(_vp)]),
+    "sblas_batch_plan_destroy": (C.c_int, [_vp]),
+    "sblas_batch_plan_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), _ip,
+                                        C.POINTER(C.c_size_t)]),
+    "sblas_batch_spmm": (C.c_int, [_vp, _vp]),
+    "sblas_batch_spmm_xy": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, C.c_int, C.c_double,
+                                      C.c_double, _vp]),
+    "sblas_batch_sddmm": (C.c_int, [_vp, _vp, C.c_int, _vp, C.c_int, _vp, _vp]),
+    "sblas_csr_transpose_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_longlong]),
+    "sblas_csr_transpose": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp,
+                                      _vp, C.c_size_t, _vp]),
+    "sblas_gather_values": (C.c_int, [C.c_longlong, C.c_int, _vp, _vp, _vp, _vp]),
     # include/spmv_kernel.h (reference signatures)
     "csr5_kernel": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _vp, _vp, _vp, _dp, _vp, _vp]),
     "spMV_mgpu_baseline": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,

@@ -257,6 +257,36 @@ int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_val, const i
                              csr_col, work, work_bytes, static_cast<cudaStream_t>(stream));
 }
 
+size_t sblas_csr_transpose_workspace_bytes(int m, int n, long long nnz)
+{
+    return csr_transpose_workspace_bytes(m, n, nnz);
+}
+
+int sblas_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
+                        int *t_rowptr, int *t_col, int *perm, void *work, size_t work_bytes,
+                        void *stream)
+{
+    clear_error();
+    if (t_rowptr == nullptr || (nnz > 0 && (rowptr == nullptr || col == nullptr ||
+                                            t_col == nullptr || perm == nullptr))) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_csr_transpose(m, n, nnz, rowptr, col, t_rowptr, t_col, perm, work, work_bytes,
+                                static_cast<cudaStream_t>(stream));
+}
+
+int sblas_gather_values(long long nnz, int val_kind, const void *src, const int *perm, void *dst,
+                        void *stream)
+{
+    clear_error();
+    if (nnz < 0 || (nnz > 0 && (src == nullptr || perm == nullptr || dst == nullptr))) {
+        set_error(SBLAS_ERR_ARG, "bad size or null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_gather_values(nnz, val_kind, src, perm, dst, static_cast<cudaStream_t>(stream));
+}
+
 int sblas_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
                              void *stream)
 {

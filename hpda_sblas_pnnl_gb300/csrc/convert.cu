@@ -195,6 +195,93 @@ __global__ void gather_kernel(long long nnz, const int *__restrict__ perm,
 }
 }  // namespace
 
+namespace {
+// Entry q of A^T is entry perm[q] of A: its column in A^T is the row of A
+// holding position perm[q] (largest r with rowptr[r] <= perm[q]).
+__global__ void transpose_rows_kernel(int m, long long nnz, const int *__restrict__ rowptr,
+                                      const int *__restrict__ perm, int *__restrict__ t_col)
+{
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nnz;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int p = __ldg(perm + q);
+        int lo = 0, hi = m - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rowptr + mid) <= p) lo = mid; else hi = mid - 1;
+        }
+        t_col[q] = lo;
+    }
+}
+
+__global__ void gather_f32_kernel(long long nnz, const int *__restrict__ perm,
+                                  const float *__restrict__ in, float *__restrict__ out)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (long long)gridDim.x * blockDim.x)
+        out[p] = __ldg(in + __ldg(perm + p));
+}
+}  // namespace
+
+size_t csr_transpose_workspace_bytes(int m, int n, long long nnz)
+{
+    (void)m;
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(n));
+    return al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+}
+
+int launch_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
+                         int *t_rowptr, int *t_col, int *perm, void *work, size_t work_bytes,
+                         cudaStream_t stream)
+{
+    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL) {
+        set_error(SBLAS_ERR_ARG, "bad sizes m=%d n=%d nnz=%lld", m, n, nnz);
+        return SBLAS_ERR_ARG;
+    }
+    if (nnz == 0) return launch_coo_rows_to_rowptr(n, 0, nullptr, t_rowptr, stream);
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
+                                              (int *)nullptr, (const int *)nullptr,
+                                              (int *)nullptr, (int)nnz, 0, end_bit_for(n));
+    const size_t need = al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)nnz);
+    if (work == nullptr || work_bytes < need) {
+        set_error(SBLAS_ERR_ARG, "csr_transpose workspace too small (%zu < %zu)", work_bytes, need);
+        return SBLAS_ERR_ARG;
+    }
+    unsigned char *w = static_cast<unsigned char *>(work);
+    int *iota = reinterpret_cast<int *>(w + al256(cub_bytes));
+    int *cols_sorted = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * nnz));
+    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, iota);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    // stable sort by column: entries of one column keep their row order
+    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(w, cub_bytes, col, cols_sorted, iota,
+                                                              perm, (int)nnz, 0, end_bit_for(n),
+                                                              stream)));
+    transpose_rows_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(m, nnz, rowptr, perm, t_col);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return launch_coo_rows_to_rowptr(n, nnz, cols_sorted, t_rowptr, stream);
+}
+
+int launch_gather_values(long long nnz, int val_kind, const void *src, const int *perm, void *dst,
+                         cudaStream_t stream)
+{
+    if (nnz <= 0) return SBLAS_OK;
+    if (val_kind == VAL_F64)
+        return launch_gather(nnz, perm, nullptr, nullptr, static_cast<const double *>(src),
+                             static_cast<double *>(dst), stream);
+    if (val_kind != VAL_F32) {
+        set_error(SBLAS_ERR_ARG, "values of kind %d cannot be gathered", val_kind);
+        return SBLAS_ERR_ARG;
+    }
+    gather_f32_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, perm,
+                                                               static_cast<const float *>(src),
+                                                               static_cast<float *>(dst));
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
 int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
                   const double *in_d, double *out_d, cudaStream_t stream)
 {

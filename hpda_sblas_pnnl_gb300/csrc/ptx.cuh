@@ -122,11 +122,12 @@ __device__ __forceinline__ double ldg_x_issue(const double *p, uint64_t policy)
     return v;
 }
 
-__device__ __forceinline__ float2 ldg_x2(const float2 *p, uint64_t policy)
+// 16-byte gather (two consecutive right-hand-side columns of one row of X)
+__device__ __forceinline__ double2 ldg_x2(const double2 *p, uint64_t policy)
 {
-    float2 v;
-    asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
-                 : "=f"(v.x), "=f"(v.y)
+    double2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                 : "=d"(v.x), "=d"(v.y)
                  : "l"(p), "l"(policy));
     return v;
 }

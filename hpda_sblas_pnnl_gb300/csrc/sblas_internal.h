@@ -44,8 +44,8 @@ int tile_shape_index(int sigma);   // -1 if not compiled
 
 size_t tile_workspace_bytes(long long nnz, int sigma);
 
-// Value storage of the matrix:  0 = FP64, 1 = FP32 (accumulated in FP64
-// through a double-float product and run sum), 2 = pattern (no value array).
+// Value storage of the matrix:  0 = FP64, 1 = FP32 (widened to FP64, products
+// and sums in FP64), 2 = pattern (no value array; every stored entry is 1).
 enum ValueKind { VAL_F64 = 0, VAL_F32 = 1, VAL_PATTERN = 2 };
 
 // Launches partition + tile kernel + carry fix-up on `stream`.
@@ -73,6 +73,13 @@ int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *row
                               cudaStream_t stream);
 // CSC -> CSR transpose (stable: columns ascending inside each row).
 size_t csc_to_csr_workspace_bytes(int m, int n, long long nnz);
+// CSR structure of A -> CSR structure of A^T plus the permutation of values.
+size_t csr_transpose_workspace_bytes(int m, int n, long long nnz);
+int launch_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
+                         int *t_rowptr, int *t_col, int *perm, void *work, size_t work_bytes,
+                         cudaStream_t stream);
+int launch_gather_values(long long nnz, int val_kind, const void *src, const int *perm, void *dst,
+                         cudaStream_t stream);
 int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
                       const int *csc_colptr, const int *csc_row, double *csr_val,
                       int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,

@@ -1,0 +1,601 @@
+// Batched CSR SpMM: many matrices of uneven size, K right-hand sides each,
+// in one persistent launch (plus a short carry fix-up), the form the
+// reference's task-pool schedule takes on one GPU
+// (reference: src/dspmv_mgpu_v2.cu:103-307 hands nnz chunks of `nb` to a pool
+// of streams; include/spmv_task.h:4-36 is the task record).
+//
+// Work unit: 32 * S consecutive nonzeros of one matrix, one warp.  Lane l
+// owns nonzeros [U0 + l*S, U0 + l*S + S) and accumulates them sequentially in
+// FP64 (K independent chains, one per right-hand side).  For every nonzero
+// the K values of row col[j] of X are gathered as one contiguous 8K-byte
+// piece (X row-major), so K right-hand sides cost one gather, not K.
+//
+// Rows:
+//   - a row that starts and ends inside one lane's chunk goes to the warp's
+//     row buffer in shared memory;
+//   - a row crossing lanes: each lane keeps its last partial (tail) and its
+//     first segment (head); a segmented shuffle scan over the tails joins
+//     them (run only when some row spans three or more lanes);
+//   - a row crossing units: the unit's first-row partial (head) and
+//     last-row partial (tail) go to per-unit carry arrays, and the fix-up
+//     kernel adds, for every head, the tails of the preceding units of the
+//     same row, in a fixed order (deterministic, no atomics);
+//   - the unit's completed rows are written out by the whole warp at the
+//     end (coalesced), alpha and beta applied once per row and column.
+// Units with more rows than the row buffer holds, or with empty rows inside
+// a chunk, take a per-lane general path with the same results.
+#pragma once
+
+#include <climits>
+
+#include "ptx.cuh"
+#include "sblas_internal.h"
+
+namespace sblas {
+namespace batch {
+
+constexpr int NW = 4;                 // warps per CTA
+constexpr int CTA = NW * 32;
+
+// device copy of one sblas_batch_matrix, plus its place in the unit list
+struct Mat {
+    const void *val;
+    const int *rowptr;
+    const int *col;
+    const double *x;
+    double *y;
+    long long nnz;
+    int m;
+    int n;
+    int ldx;
+    int ldy;
+    double alpha;
+    double beta;
+    int unit0;    // first unit of this matrix
+    int nunits;   // units of this matrix (>= 1, also for nnz == 0)
+};
+
+struct Args {
+    const Mat *mats;
+    int nmat;
+    const int *unit_mat;   // [nunits] matrix of each unit
+    const int *unit_row;   // [nunits] first row of each unit
+    int *head_row;         // [nunits] row of the unit's head carry, -1: none
+    double *head_val;      // [nunits * K]
+    int *tail_row;         // [nunits] row of the unit's tail carry, -1: none
+    double *tail_val;      // [nunits * K]
+    int nunits;
+    // single-matrix calls: X, Y, alpha, beta (and optionally the values)
+    // given per call
+    int override_xy;
+    const double *x;
+    double *y;
+    int ldx;
+    int ldy;
+    double alpha;
+    double beta;
+    const void *val;       // nullptr: the plan's values
+    // sampled product (adjoint of the values): dval[p] = G[row(p),:] . X[col(p),:]
+    const double *g;
+    int ldg;
+    void *dval;            // FP64 or FP32 per the value kind
+};
+
+template <int K, int S>
+struct Shape {
+    static constexpr int UNIT = 32 * S;                        // nonzeros per unit
+    static constexpr int RCAP = (8 * S < 1024 / K) ? 8 * S : 1024 / K;  // rows in the buffer
+    static constexpr int RPN = RCAP + 2;                       // row-pointer slice entries
+};
+
+template <int VK>
+struct VT;
+template <>
+struct VT<VAL_F64> {
+    using T = double;
+    static constexpr int B = 8;
+};
+template <>
+struct VT<VAL_F32> {
+    using T = float;
+    static constexpr int B = 4;
+};
+template <>
+struct VT<VAL_PATTERN> {
+    using T = float;   // unused
+    static constexpr int B = 0;
+};
+
+// shared memory of one warp
+template <int K, int S, int VK>
+struct WarpSmem {
+    using SH = Shape<K, S>;
+    static constexpr size_t COL = 0;
+    static constexpr size_t VAL = COL + size_t(SH::UNIT) * 4;
+    static constexpr size_t RP = (VAL + size_t(SH::UNIT) * VT<VK>::B + 15) / 16 * 16;
+    static constexpr size_t RBUF = (RP + size_t(SH::RPN) * 4 + 15) / 16 * 16;
+    static constexpr size_t HBUF = RBUF + size_t(SH::RCAP) * K * 8;
+    static constexpr size_t TOTAL = HBUF + size_t(32) * K * 8;
+};
+
+template <int K, int S, int VK>
+constexpr size_t cta_smem_bytes()
+{
+    return size_t(NW) * WarpSmem<K, S, VK>::TOTAL;
+}
+
+// FP32 value widened to FP64 with integer operations (exact for every float
+// class; the FP64 pipe stays free for the multiply-adds)
+__device__ __forceinline__ double widen(float v)
+{
+    const unsigned u0 = __float_as_uint(v);
+    const bool sub = (u0 & 0x7F800000u) == 0u && (u0 << 1) != 0u;
+    const unsigned u = sub ? __float_as_uint(v * 0x1p64f) : u0;
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned ed = (e == 0xFFu) ? 0x7FFu : (e == 0u ? 0u : e + 896u - (sub ? 64u : 0u));
+    const unsigned hi = (u & 0x80000000u) | (ed << 20) | ((u >> 3) & 0xFFFFFu);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+template <int VK>
+__device__ __forceinline__ double value_at(const void *v)
+{
+    if constexpr (VK == VAL_F64) return *static_cast<const double *>(v);
+    else if constexpr (VK == VAL_F32) return widen(*static_cast<const float *>(v));
+    else return 1.0;
+}
+
+// K consecutive doubles of row c of X (16-byte aligned when K >= 2)
+template <int K>
+__device__ __forceinline__ void gather_row(const double *x, long long c, int ldx, double (&r)[K],
+                                           uint64_t pol)
+{
+    const double *p = x + c * ldx;
+    if constexpr (K == 1) {
+        r[0] = ptx::ldg_x_issue(p, pol);
+    } else {
+#pragma unroll
+        for (int q = 0; q < K / 2; ++q) {
+            const double2 v = ptx::ldg_x2(reinterpret_cast<const double2 *>(p) + q, pol);
+            r[2 * q] = v.x;
+            r[2 * q + 1] = v.y;
+        }
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void store_row(double *dst, const double (&a)[K])
+{
+    if constexpr (K == 1) {
+        dst[0] = a[0];
+    } else {
+#pragma unroll
+        for (int q = 0; q < K / 2; ++q)
+            reinterpret_cast<double2 *>(dst)[q] = make_double2(a[2 * q], a[2 * q + 1]);
+    }
+}
+
+__device__ __forceinline__ double finish(double v, double alpha, double beta, const double *yp)
+{
+    return beta == 0.0 ? alpha * v : fma(alpha, v, beta * *yp);
+}
+
+// ---- main kernel: persistent, one warp per unit, units round-robin ---------
+template <int K, int S, int VK>
+__global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
+{
+    using SH = Shape<K, S>;
+    using WS = WarpSmem<K, S, VK>;
+    using T = typename VT<VK>::T;
+    static_assert(S <= 32, "row-start mask is 32 bits");
+    static_assert(K == 1 || K % 2 == 0, "K is 1 or even");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *ws = smem_raw + size_t(warp) * WS::TOTAL;
+    int *scol = reinterpret_cast<int *>(ws + WS::COL);
+    T *sval = reinterpret_cast<T *>(ws + WS::VAL);
+    int *srp = reinterpret_cast<int *>(ws + WS::RP);
+    double *rbuf = reinterpret_cast<double *>(ws + WS::RBUF);
+    double *hbuf = reinterpret_cast<double *>(ws + WS::HBUF) + lane * K;
+    const uint64_t pol_x = ptx::policy_evict_last();
+    const unsigned FULL = 0xffffffffu;
+
+    for (int u = blockIdx.x * NW + warp; u < a.nunits; u += gridDim.x * NW) {
+        const int b = __ldg(a.unit_mat + u);
+        const Mat *M = a.mats + b;
+        const int *rowptr = M->rowptr;
+        const int *col = M->col;
+        const void *val = (a.override_xy && a.val) ? a.val : M->val;
+        const double *x = a.override_xy ? a.x : M->x;
+        double *y = a.override_xy ? a.y : M->y;
+        const int ldx = a.override_xy ? a.ldx : M->ldx;
+        const int ldy = a.override_xy ? a.ldy : M->ldy;
+        const double alpha = a.override_xy ? a.alpha : M->alpha;
+        const double beta = a.override_xy ? a.beta : M->beta;
+        const int m = M->m;
+        const int lu = u - M->unit0;
+        const int U0 = lu * SH::UNIT;   // row pointers are int32: nnz < 2^31
+        const int cntu = (int)min((long long)SH::UNIT, M->nnz - U0);
+        const int RA = __ldg(a.unit_row + u);
+        const int RB = (lu + 1 < M->nunits) ? __ldg(a.unit_row + u + 1) : m;
+        const int nrows = RB - RA;
+        const bool fits = nrows <= SH::RCAP;
+        const int rp_hi = min(RB + 1, m);   // highest row-pointer index read
+
+        // ---- stage the unit (coalesced), zero the row buffer ------------
+        __syncwarp();
+        for (int i = lane; i < cntu; i += 32) scol[i] = __ldcs(col + U0 + i);
+        if constexpr (VK != VAL_PATTERN)
+            for (int i = lane; i < cntu; i += 32) sval[i] = __ldcs(static_cast<const T *>(val) + U0 + i);
+        if (fits) {
+            for (int i = lane; i <= rp_hi - RA; i += 32) srp[i] = __ldg(rowptr + RA + i);
+            for (int i = lane; i < nrows * K; i += 32) rbuf[i] = 0.0;
+        }
+        __syncwarp();
+        auto rp = [&](int r) -> int { return fits ? srp[r - RA] : __ldg(rowptr + r); };
+
+        // ---- this lane's chunk ------------------------------------------
+        const int c0 = lane * S;
+        const int cnt = max(0, min(S, cntu - c0));
+        const int s0 = U0 + c0, send = s0 + cnt;
+        double xs[K == 1 ? S : 1];       // K == 1: every gather issued up front
+        double cur[K];                   // K >= 2: one row of X ahead
+        if (cnt > 0) {
+            if constexpr (K == 1) {
+#pragma unroll
+                for (int j = 0; j < S; ++j)
+                    xs[j] = ptx::ldg_x_issue(x + (long long)scol[c0 + (j < cnt ? j : 0)] * ldx, pol_x);
+            } else {
+                gather_row<K>(x, scol[c0], ldx, cur, pol_x);
+            }
+        }
+        int r0 = RA, rl = RA;
+        bool sb = false, ends = false, slow = !fits;
+        unsigned mask = 0;
+        if (cnt > 0) {
+            int lo = RA, hi = min(RB, m - 1);
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rp(mid) <= s0) lo = mid; else hi = mid - 1;
+            }
+            r0 = lo;
+            sb = rp(r0) < s0;
+            int rr = r0, nx = rp(r0 + 1);
+            while (nx < send) {
+                mask |= 1u << (nx - s0);
+                const int n2 = rp(rr + 2);
+                slow |= (n2 == nx);      // an empty row inside the chunk
+                ++rr;
+                nx = n2;
+            }
+            rl = rr;
+            ends = (nx == send);
+        }
+        const bool warp_slow = __any_sync(FULL, slow);
+
+        double acc[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) acc[c] = 0.0;
+        bool has_head = false, has_tail = false, mid_lane = false;
+        int hrow = -1, trow = -1;
+
+        auto fma_row = [&](int j, const double (&xr)[K]) {
+            const double v = value_at<VK>(sval + c0 + j);
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                if constexpr (VK == VAL_PATTERN) acc[c] += xr[c];
+                else acc[c] = fma(v, xr[c], acc[c]);
+            }
+        };
+        auto step = [&](int j) {
+            if constexpr (K == 1) {
+                const double xr[1] = {xs[j]};
+                fma_row(j, xr);
+            } else {
+                double nxt[K];
+                if (j + 1 < cnt) gather_row<K>(x, scol[c0 + j + 1], ldx, nxt, pol_x);
+                fma_row(j, cur);
+#pragma unroll
+                for (int c = 0; c < K; ++c) cur[c] = nxt[c];
+            }
+        };
+
+        if (cnt > 0 && !warp_slow) {
+            // branch-free row emission: at a row start the running sums go to
+            // the row buffer (or the head slot for a row begun before the
+            // chunk) and restart
+            double *dst = sb ? hbuf : rbuf + (r0 - RA) * K;
+            double *nxp = rbuf + (r0 + 1 - RA) * K;
+#pragma unroll
+            for (int j = 0; j < S; ++j) {
+                const bool bnd = (mask >> j) & 1u;
+                if (bnd) store_row<K>(dst, acc);
+                dst = bnd ? nxp : dst;
+                nxp = bnd ? nxp + K : nxp;
+#pragma unroll
+                for (int c = 0; c < K; ++c) acc[c] = bnd ? 0.0 : acc[c];
+                if (j < cnt) step(j);
+            }
+            if (ends) store_row<K>(dst, acc);
+            has_head = sb && (mask != 0u || ends);
+            hrow = r0;
+            has_tail = !ends;
+            trow = rl;
+            mid_lane = has_tail && sb && mask == 0u;
+        } else if (cnt > 0) {
+            // general path: empty rows inside the chunk, or more rows than
+            // the row buffer holds (rows then go straight to y)
+            int r = r0, next = rp(r0 + 1);
+            bool first = true;
+            auto emit = [&](int row) {
+                if (first && sb) {
+                    store_row<K>(hbuf, acc);
+                    has_head = true;
+                    hrow = row;
+                } else if (fits) {
+                    store_row<K>(rbuf + (row - RA) * K, acc);
+                } else {
+                    double *yr = y + (long long)row * ldy;
+#pragma unroll
+                    for (int c = 0; c < K; ++c) yr[c] = finish(acc[c], alpha, beta, yr + c);
+                }
+                first = false;
+#pragma unroll
+                for (int c = 0; c < K; ++c) acc[c] = 0.0;
+            };
+#pragma unroll
+            for (int j = 0; j < S; ++j) {
+                if (j < cnt) {
+                    const int k = s0 + j;
+                    if (next == k) {
+                        emit(r);              // row r ends before nonzero k
+                        ++r;
+                        next = rp(r + 1);
+                        while (next == k) {   // empty rows: written by the epilogue
+                            ++r;
+                            next = rp(r + 1);
+                        }
+                    }
+                    step(j);
+                }
+            }
+            if (next == send) {
+                emit(r);
+                ends = true;
+            } else {
+                has_tail = true;
+                trow = r;
+                mid_lane = first && sb;
+            }
+        }
+
+        // ---- rows crossing lanes: segmented scan of the tails -------------
+        double sv[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) sv[c] = has_tail ? acc[c] : 0.0;
+        if (!has_tail) trow = -1;
+        const int trow_prev = __shfl_up_sync(FULL, trow, 1);
+        const bool cont = mid_lane && lane > 0 && trow_prev == trow;
+        if (__any_sync(FULL, cont)) {
+            bool f = !cont;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const bool fo = __shfl_up_sync(FULL, f, d);
+                const bool take = (lane >= d) && !f;
+#pragma unroll
+                for (int c = 0; c < K; ++c) {
+                    const double so = __shfl_up_sync(FULL, sv[c], d);
+                    sv[c] += take ? so : 0.0;
+                }
+                f = take ? fo : f;
+            }
+        }
+        double sprev[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) sprev[c] = __shfl_up_sync(FULL, sv[c], 1);
+        const bool join = has_head && lane > 0 && trow_prev == hrow;
+        const bool head_before_unit = has_head && hrow == RA && rp(RA) < U0;
+        if (has_head) {
+            double tot[K];
+#pragma unroll
+            for (int c = 0; c < K; ++c) tot[c] = hbuf[c] + (join ? sprev[c] : 0.0);
+            if (head_before_unit) {
+                a.head_row[u] = hrow;
+                store_row<K>(a.head_val + (long long)u * K, tot);
+            } else if (fits) {
+                store_row<K>(rbuf + (hrow - RA) * K, tot);
+            } else {
+                double *yr = y + (long long)hrow * ldy;
+#pragma unroll
+                for (int c = 0; c < K; ++c) yr[c] = finish(tot[c], alpha, beta, yr + c);
+            }
+        }
+        const int last = cntu > 0 ? (cntu - 1) / S : 0;
+        const bool unit_tail = lane == last && has_tail;
+        if (unit_tail) {
+            a.tail_row[u] = trow;
+            store_row<K>(a.tail_val + (long long)u * K, sv);
+        }
+        const unsigned hb = __ballot_sync(FULL, head_before_unit);
+        const unsigned tb = __ballot_sync(FULL, unit_tail);
+        if (lane == 0) {
+            if (hb == 0u) a.head_row[u] = -1;
+            if (tb == 0u) a.tail_row[u] = -1;
+        }
+        __syncwarp();
+
+        // ---- epilogue: the unit's complete rows, coalesced -----------------
+        const int E0 = (rp(RA) < U0) ? RA + 1 : RA;
+        if (fits) {
+            const int ne = (RB - E0) * K;
+            for (int i = lane; i < ne; i += 32) {
+                const int rr = i / K, c = i - rr * K;
+                double *yp = y + (long long)(E0 + rr) * ldy + c;
+                *yp = finish(rbuf[(E0 - RA + rr) * K + c], alpha, beta, yp);
+            }
+        } else {
+            for (int r = E0 + lane; r < RB; r += 32)
+                if (__ldg(rowptr + r) == __ldg(rowptr + r + 1)) {
+                    double *yr = y + (long long)r * ldy;
+#pragma unroll
+                    for (int c = 0; c < K; ++c) yr[c] = finish(0.0, alpha, beta, yr + c);
+                }
+        }
+    }
+}
+
+// ---- carry fix-up: rows crossing units ------------------------------------
+// For every unit whose first row began in an earlier unit: that row's total
+// is the unit's head plus the tails of the preceding units on the same row,
+// added nearest first.
+template <int K>
+__global__ void batch_fixup_kernel(const Args a)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.nunits;
+         u += gridDim.x * blockDim.x) {
+        const int R = a.head_row[u];
+        if (R < 0) continue;
+        const Mat *M = a.mats + __ldg(a.unit_mat + u);
+        double t[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) t[c] = a.head_val[(long long)u * K + c];
+        for (int v = u - 1; v >= M->unit0 && a.tail_row[v] == R; --v) {
+#pragma unroll
+            for (int c = 0; c < K; ++c) t[c] += a.tail_val[(long long)v * K + c];
+        }
+        double *y = a.override_xy ? a.y : M->y;
+        const int ldy = a.override_xy ? a.ldy : M->ldy;
+        const double alpha = a.override_xy ? a.alpha : M->alpha;
+        const double beta = a.override_xy ? a.beta : M->beta;
+        double *yr = y + (long long)R * ldy;
+#pragma unroll
+        for (int c = 0; c < K; ++c) yr[c] = finish(t[c], alpha, beta, yr + c);
+    }
+}
+
+// ---- sampled dense-dense product over the pattern (values' adjoint) -------
+// dval[p] = sum over c of G[row(p), c] * X[col(p), c] for every stored entry
+// of a single-matrix plan; one warp per unit, lane l takes nonzeros
+// U0 + l, U0 + l + 32, ... (coalesced col and dval), rows found by a binary
+// search for the first and a forward walk after that.
+template <int K, int S, int VK>
+__global__ void __launch_bounds__(CTA) batch_sddmm_kernel(const Args a)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t pol = ptx::policy_evict_last();
+    for (int u = blockIdx.x * NW + warp; u < a.nunits; u += gridDim.x * NW) {
+        const Mat *M = a.mats + __ldg(a.unit_mat + u);
+        const int *rowptr = M->rowptr;
+        const int *col = M->col;
+        const int lu = u - M->unit0;
+        const int U0 = lu * Shape<K, S>::UNIT;
+        const int cntu = (int)min((long long)Shape<K, S>::UNIT, M->nnz - U0);
+        if (lane >= cntu) continue;
+        const int RA = __ldg(a.unit_row + u);
+        const int RB = (lu + 1 < M->nunits) ? __ldg(a.unit_row + u + 1) : M->m - 1;
+        int p = U0 + lane;
+        int lo = RA, hi = min(RB, M->m - 1);
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rowptr + mid) <= p) lo = mid; else hi = mid - 1;
+        }
+        int r = lo;
+        int next = __ldg(rowptr + r + 1);
+        for (int i = lane; i < cntu; i += 32, p += 32) {
+            while (next <= p) {
+                ++r;
+                next = __ldg(rowptr + r + 1);
+            }
+            double gr[K], xr[K];
+            gather_row<K>(a.g, r, a.ldg, gr, pol);
+            gather_row<K>(a.x, __ldcs(col + p), a.ldx, xr, pol);
+            double d = 0.0;
+#pragma unroll
+            for (int c = 0; c < K; ++c) d = fma(gr[c], xr[c], d);
+            if constexpr (VK == VAL_F32) static_cast<float *>(a.dval)[p] = (float)d;
+            else static_cast<double *>(a.dval)[p] = d;
+        }
+    }
+}
+
+// Launch of one compiled shape (main kernel + fix-up) on `stream`.
+template <int K, int S, int VK>
+cudaError_t launch_shape(const Args &a, int grid, cudaStream_t stream)
+{
+    constexpr size_t smem = cta_smem_bytes<K, S, VK>();
+    if (a.nunits <= 0) return cudaSuccess;
+    batch_spmm_kernel<K, S, VK><<<grid, CTA, smem, stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int fgrid = (a.nunits + 255) / 256 < 1024 ? (a.nunits + 255) / 256 : 1024;
+    batch_fixup_kernel<K><<<fgrid, 256, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Occupancy-sized persistent grid for one compiled shape (sets the dynamic
+// shared-memory limit of the kernel first).
+template <int K, int S, int VK>
+cudaError_t shape_grid(int nunits, int *grid)
+{
+    constexpr size_t smem = cta_smem_bytes<K, S, VK>();
+    auto kfn = batch_spmm_kernel<K, S, VK>;
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, bps = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA, smem)) != cudaSuccess)
+        return e;
+    if (bps < 1) return cudaErrorInvalidConfiguration;
+    const long long need = (nunits + NW - 1) / NW;
+    const long long full = (long long)sms * bps;
+    *grid = (int)(need < full ? need : full);
+    if (*grid < 1) *grid = 1;
+    return cudaSuccess;
+}
+
+}  // namespace batch
+}  // namespace sblas
+
+namespace sblas {
+namespace batch {
+
+// Compiled shapes: K in {1, 2, 4, 8, 16} (one translation unit each),
+// S in {4, 8, 16, 32}, every value kind.  Op::GRID computes the persistent
+// grid of the shape into *grid_out; SPMM and SDDMM launch.
+template <int K, int S, int VK>
+cudaError_t launch_sddmm(const Args &a, int grid, cudaStream_t stream)
+{
+    if constexpr (VK == VAL_PATTERN) {
+        return cudaErrorInvalidValue;
+    } else {
+        if (a.nunits <= 0) return cudaSuccess;
+        batch_sddmm_kernel<K, S, VK><<<grid, CTA, 0, stream>>>(a);
+        return cudaGetLastError();
+    }
+}
+
+enum class Op { GRID, SPMM, SDDMM };
+
+template <int K>
+cudaError_t dispatch_k(Op op, int S, int VK, const Args *a, int nunits, int grid, int *grid_out,
+                       cudaStream_t stream)
+{
+#define SBLAS_BATCH_SHAPE(SS, VV)                                                        \
+    if (S == SS && VK == VV)                                                             \
+        return op == Op::SPMM    ? launch_shape<K, SS, VV>(*a, grid, stream)             \
+               : op == Op::SDDMM ? launch_sddmm<K, SS, VV>(*a, grid, stream)             \
+                                 : shape_grid<K, SS, VV>(nunits, grid_out);
+#define SBLAS_BATCH_S(SS)                                                                \
+    SBLAS_BATCH_SHAPE(SS, VAL_F64) SBLAS_BATCH_SHAPE(SS, VAL_F32) SBLAS_BATCH_SHAPE(SS, VAL_PATTERN)
+    SBLAS_BATCH_S(4)
+    SBLAS_BATCH_S(8)
+    SBLAS_BATCH_S(16)
+    SBLAS_BATCH_S(32)
+#undef SBLAS_BATCH_S
+#undef SBLAS_BATCH_SHAPE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace batch
+}  // namespace sblas

@@ -81,10 +81,7 @@ struct Layout {
     static constexpr size_t META = align16(RPTR + size_t(STAGES) * RSLOT * 4);
     // carry buffers, double-buffered by tile parity
     static constexpr size_t RVAL = align16(META + size_t(STAGES) * 16);
-    // float-pair row sums written by the double-float forms (FP32 values,
-    // pattern-only); absent for FP64
-    static constexpr size_t RVF = align16(RVAL + 2 * size_t(RCAP) * 8);
-    static constexpr size_t TAILV = align16(RVF + (VK == VAL_F64 ? 0 : 2 * size_t(RCAP) * 8));
+    static constexpr size_t TAILV = align16(RVAL + 2 * size_t(RCAP) * 8);
     static constexpr size_t HEADV = TAILV + 2 * size_t(TC) * 8;
     static constexpr size_t CIN = HEADV + 2 * size_t(TC) * 8;
     static constexpr size_t TAILK = CIN + size_t(TC) * 8;
@@ -134,7 +131,6 @@ struct Smem {
     __device__ int *rptr(int s) const { return reinterpret_cast<int *>(base + L::RPTR) + size_t(s) * L::RSLOT; }
     __device__ int *meta(int s) const { return reinterpret_cast<int *>(base + L::META) + 4 * s; }
     __device__ double *rval(int p) const { return reinterpret_cast<double *>(base + L::RVAL) + size_t(p) * L::RCAP; }
-    __device__ float2 *rvf(int p) const { return reinterpret_cast<float2 *>(base + L::RVF) + size_t(p) * L::RCAP; }
     __device__ double *tailv(int p) const { return reinterpret_cast<double *>(base + L::TAILV) + p * TC; }
     __device__ double *headv(int p) const { return reinterpret_cast<double *>(base + L::HEADV) + p * TC; }
     __device__ double *cin() const { return reinterpret_cast<double *>(base + L::CIN); }
@@ -205,46 +201,21 @@ __device__ __forceinline__ void produce_tile(const TileArgs &a, const Smem<SIGMA
     }
 }
 
-// ---- double-float arithmetic for the FP32-value and pattern-only forms ----
-// F2F conversions run on the FP64 pipe on this GPU, so these forms keep the
-// per-nonzero work on the FP32 and integer pipes: x is split into hi + lo
-// floats with integer operations and one I2F (hi = x with its significand
-// cut to 24 bits, lo = the remaining 29 bits rounded to 24: |x - hi - lo| <=
-// 2^-47 |x|), each product is formed exactly in two floats (FMA error term)
-// and the chunk's running sums are kept as float pairs with TwoSum
-// (Knuth; ~48-bit significand).  Chunk results are converted to FP64 once;
-// carries and row sums are FP64.  ok: |x| in [2^-60, 2^61) or x == 0.
-__device__ __forceinline__ void df_split(double x, float &hi, float &lo, bool &ok)
+// FP32 value widened to FP64 exactly with integer operations: sign, the
+// exponent rebased by 1023 - 127 (2047 for infinities and NaNs), the 23-bit
+// significand moved to the top of the 52-bit field; a subnormal is first
+// scaled by 2^64 in FP32 (exact) and its exponent lowered by 64 again.  F2F
+// conversions run on the FP64 pipe of this GPU, which the multiply-adds
+// already keep busy; these run on the integer and FP32 pipes.
+__device__ __forceinline__ double widen_f32(float v)
 {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
-    const unsigned e = (h32 >> 20) & 0x7FFu;
-    const unsigned sign = h32 & 0x80000000u;
-    const bool zero = (b << 1) == 0ull;
-    ok = zero || (e >= 963u && e <= 1083u);
-    const unsigned hb = sign | (((e - 896u) & 0xFFu) << 23) | ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
-    const float r = __uint2float_rn(l32 & 0x1FFFFFFFu);
-    const float sc = __uint_as_float(((e - 948u) & 0xFFu) << 23);   // 2^(e-1075)
-    const float l = r * sc;
-    hi = zero ? 0.0f : __uint_as_float(hb);
-    lo = zero ? 0.0f : __uint_as_float(__float_as_uint(l) | sign);
-}
-
-// FP32 value usable on the double-float path: 0 or |v| in [2^-60, 2^61)
-__device__ __forceinline__ bool df_value_ok(float v)
-{
-    const unsigned e = (__float_as_uint(v) >> 23) & 0xFFu;
-    return ((__float_as_uint(v) << 1) == 0u) || (e >= 67u && e <= 187u);
-}
-
-// (sh, sl) += (ph, pl) with TwoSum on the high parts
-__device__ __forceinline__ void df_acc(float &sh, float &sl, float ph, float pl)
-{
-    const float s = sh + ph;
-    const float bv = s - sh;
-    const float err = (sh - (s - bv)) + (ph - bv);
-    sh = s;
-    sl += err + pl;
+    const unsigned u0 = __float_as_uint(v);
+    const bool sub = (u0 & 0x7F800000u) == 0u && (u0 << 1) != 0u;
+    const unsigned u = sub ? __float_as_uint(v * 0x1p64f) : u0;
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned ed = (e == 0xFFu) ? 0x7FFu : (e == 0u ? 0u : e + 896u - (sub ? 64u : 0u));
+    const unsigned hi = (u & 0x80000000u) | (ed << 20) | ((u >> 3) & 0xFFFFFu);
+    return __hiloint2double((int)hi, (int)(u << 29));
 }
 
 // Compute warp: for each tile of the CTA, one chunk of SIGMA consecutive
@@ -331,62 +302,7 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
         int head_row = -1;
         double head_val = 0.0;
         double *headv = sm.headv(p);
-        // double-float forms: split x, check the operands' range (the warp
-        // falls back to FP64 arithmetic if any is out of range)
-        float xh[VK == VAL_F64 ? 1 : SIGMA], xl[VK == VAL_F64 ? 1 : SIGMA];
-        bool df_ok = (VK != VAL_F64);
-        if constexpr (VK != VAL_F64) {
-            bool okl = true;
-            if (cnt > 0) {
-#pragma unroll
-                for (int j = 0; j < SIGMA; ++j) {
-                    bool okx;
-                    df_split(xv[j], xh[j], xl[j], okx);
-                    if (j < cnt) {
-                        okl = okl && okx;
-                        if (VK == VAL_F32) okl = okl && df_value_ok((float)vst[c0 + j]);
-                    }
-                }
-            }
-            df_ok = __all_sync(0xffffffffu, okl);
-        }
-        if (VK != VAL_F64 && cnt > 0 && !warp_slow && df_ok) {
-            // double-float chain: FP32/integer pipes only; the chunk's row
-            // sums are stored as float pairs (converted in the epilogue)
-            float2 *rvf = sm.rvf(p);
-            float2 *dst = sb ? reinterpret_cast<float2 *>(&headv[t]) : &rvf[r0 - R0];
-            float2 *nxt = &rvf[r0 + 1 - R0];
-            float sh = 0.0f, sl = 0.0f;
-#pragma unroll
-            for (int j = 0; j < SIGMA; ++j) {
-                const bool b = (mask >> j) & 1u;
-                if (b) *dst = make_float2(sh, sl);
-                dst = b ? nxt : dst;
-                nxt = b ? nxt + 1 : nxt;
-                sh = b ? 0.0f : sh;
-                sl = b ? 0.0f : sl;
-                if (j < cnt) {
-                    float ph, pl;
-                    if (VK == VAL_PATTERN) {
-                        ph = xh[j];
-                        pl = xl[j];
-                    } else {
-                        const float v = (float)vst[c0 + j];
-                        ph = v * xh[j];
-                        pl = fmaf(v, xh[j], -ph);
-                        pl = fmaf(v, xl[j], pl);
-                    }
-                    df_acc(sh, sl, ph, pl);
-                }
-            }
-            sum = (double)sh + (double)sl;
-            if (sb && mask != 0u) {
-                head_row = r0;
-                const float2 hf = *reinterpret_cast<const float2 *>(&headv[t]);
-                head_val = (double)hf.x + (double)hf.y;
-                headv[t] = head_val;
-            }
-        } else if (VK == VAL_F64 && cnt > 0 && !warp_slow) {
+        if (cnt > 0 && !warp_slow) {
             // branch-free FMA chain: at a row start the running sum is stored
             // (the first segment to the thread's head slot when the row began
             // in an earlier chunk) and restarted with a select
@@ -400,7 +316,8 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
                 nxt = b ? nxt + 1 : nxt;
                 sum = b ? 0.0 : sum;
                 if (j < cnt) {
-                    if (VK == VAL_PATTERN) sum += xv[j];
+                    if constexpr (VK == VAL_PATTERN) sum += xv[j];
+                    else if constexpr (VK == VAL_F32) sum = fma(widen_f32(vst[c0 + j]), xv[j], sum);
                     else sum = fma((double)vst[c0 + j], xv[j], sum);
                 }
             }
@@ -614,20 +531,9 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
         // ---------------- epilogue: finished rows out, slots cleared ------
         const int nr = R1 - R0;
         if (fits) {
-            if constexpr (VK == VAL_F64) {
-                for (int r = lane; r < nr; r += 32) {
-                    a.y[R0 + r] = finish_row<AB>(rval[r], alpha, beta, a.y + R0 + r);
-                    rval[r] = 0.0;
-                }
-            } else {
-                float2 *rvf = sm.rvf(p);
-                for (int r = lane; r < nr; r += 32) {
-                    const float2 f = rvf[r];
-                    const double v = rval[r] + ((double)f.x + (double)f.y);
-                    a.y[R0 + r] = finish_row<AB>(v, alpha, beta, a.y + R0 + r);
-                    rval[r] = 0.0;
-                    rvf[r] = make_float2(0.0f, 0.0f);
-                }
+            for (int r = lane; r < nr; r += 32) {
+                a.y[R0 + r] = finish_row<AB>(rval[r], alpha, beta, a.y + R0 + r);
+                rval[r] = 0.0;
             }
         } else {
             for (int rr = R0 + lane; rr < R1; rr += 32)
@@ -667,7 +573,6 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
     if (VK != VAL_F64)
-        for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rvf(0)[i] = make_float2(0.f, 0.f);
     for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
     __syncthreads();
     if (warp == NCW)

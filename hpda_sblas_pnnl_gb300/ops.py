@@ -186,3 +186,165 @@ class CsrPlan:
                                        self.work_bytes, _stream_ptr(self.device))
         _lib.check(rc)
         return y
+
+
+def _val_kind(val: torch.Tensor | None) -> int:
+    if val is None:
+        return VAL_PATTERN
+    if val.dtype == torch.float64:
+        return VAL_F64
+    if val.dtype == torch.float32:
+        return VAL_F32
+    raise TypeError("val must be float64, float32 or None")
+
+
+def batch_default_s(k: int) -> int:
+    return int(_lib.load().sblas_batch_default_s(k))
+
+
+class BatchPlan:
+    """Many CSR matrices, k right-hand sides each: Y_i = alpha*A_i*X_i + beta*Y_i.
+
+    matrices: list of (rowptr, col, val) with int32 indices and val float64,
+    float32 or None (pattern; every matrix of a batch has the same value
+    kind).  xs[i]: float64 (n_i, k) row-major (or (n_i,) for k = 1);
+    ys[i]: float64 (m_i, k).  The plan (sblas_batch_plan_create) copies the
+    descriptors to the device and partitions all matrices into units of
+    32*s nonzeros; each call is one persistent kernel plus the carry fix-up
+    (sblas_batch_spmm): no allocation, no copy, graph-capturable.  s = 0
+    takes the library default for k (see tune.batch_s for a measured pick).
+    """
+
+    def __init__(self, matrices, xs, ys, k: int, alpha: float = 1.0, beta: float = 0.0,
+                 s: int = 0):
+        if not (len(matrices) == len(xs) == len(ys)) or not matrices:
+            raise ValueError("need one x and one y per matrix")
+        flat = [t for mat in matrices for t in mat] + list(xs) + list(ys)
+        dev = _require_cuda(*flat)
+        kinds = {_val_kind(v) for _, _, v in matrices}
+        if len(kinds) != 1:
+            raise TypeError("all matrices of a batch have the same value kind")
+        self.vk = kinds.pop()
+        self.k = int(k)
+        self.device = dev
+        self.matrices, self.xs, self.ys = list(matrices), list(xs), list(ys)
+        arr = (_lib.BatchMatrix * len(matrices))()
+        for i, ((rp, col, val), x, y) in enumerate(zip(matrices, xs, ys)):
+            if rp.dtype != torch.int32 or col.dtype != torch.int32:
+                raise TypeError("rowptr and col must be int32")
+            if x.dtype != torch.float64 or y.dtype != torch.float64:
+                raise TypeError("x and y must be float64")
+            m = rp.numel() - 1
+            n = x.shape[0]
+            if y.shape[0] != m or (x.dim() > 1 and x.shape[1] != self.k) or \
+                    (y.dim() > 1 and y.shape[1] != self.k) or (self.k > 1 and x.dim() != 2):
+                raise ValueError(f"matrix {i}: x must be (n, k) and y (m, k)")
+            arr[i] = _lib.BatchMatrix(m, n, col.numel(), _ptr(val).value, _ptr(rp).value,
+                                      _ptr(col).value, _ptr(x).value, self.k, _ptr(y).value,
+                                      self.k, float(alpha), float(beta))
+        lib = _lib.load()
+        h = C.c_void_p()
+        with torch.cuda.device(dev):
+            rc = lib.sblas_batch_plan_create(len(matrices), arr, self.k, self.vk, int(s),
+                                             _stream_ptr(dev), C.byref(h))
+        _lib.check(rc)
+        self._h = h
+        units, s_out, nbytes = C.c_longlong(), C.c_int(), C.c_size_t()
+        _lib.check(lib.sblas_batch_plan_info(h, C.byref(units), C.byref(s_out), C.byref(nbytes)))
+        self.units, self.s, self.device_bytes = units.value, s_out.value, nbytes.value
+
+    def __call__(self) -> None:
+        rc = _lib.load().sblas_batch_spmm(self._h, _stream_ptr(self.device))
+        _lib.check(rc)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().sblas_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SpmmPlan(BatchPlan):
+    """One CSR matrix with k right-hand sides, X, Y, alpha and beta given per
+    call: Y = alpha*A*X + beta*Y (sblas_batch_spmm_xy).  The structure is
+    fixed at construction; the values may be replaced per call (val=, same
+    dtype as at construction)."""
+
+    def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
+                 n: int, k: int, s: int = 0):
+        dev = _require_cuda(rowptr, col, val)
+        m = rowptr.numel() - 1
+        # placeholders fixing the shapes; every call passes its own X and Y
+        xs = torch.empty((max(n, 1), k), dtype=torch.float64, device=dev)
+        ys = torch.empty((max(m, 1), k), dtype=torch.float64, device=dev)
+        super().__init__([(rowptr, col, val)], [xs[:n]], [ys[:m]], k, s=s)
+        self.m, self.n = m, n
+        self.val_dtype = None if val is None else val.dtype
+
+    def _check_val(self, val):
+        if val is None:
+            return
+        _require_cuda(val)
+        if self.val_dtype is None or val.dtype != self.val_dtype:
+            raise TypeError("values must have the dtype the plan was built with")
+        if val.numel() != self.matrices[0][1].numel():
+            raise ValueError("one value per stored entry")
+
+    def __call__(self, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+                 val: torch.Tensor | None = None) -> torch.Tensor:
+        _require_cuda(x, y)
+        self._check_val(val)
+        if x.dtype != torch.float64 or y.dtype != torch.float64:
+            raise TypeError("x and y must be float64")
+        if x.shape[0] != self.n or y.shape[0] != self.m:
+            raise ValueError("x must be (n, k) and y (m, k)")
+        rc = _lib.load().sblas_batch_spmm_xy(self._h, _ptr(val), _ptr(x), self.k, _ptr(y),
+                                             self.k, float(alpha), float(beta),
+                                             _stream_ptr(self.device))
+        _lib.check(rc)
+        return y
+
+    def sddmm(self, g: torch.Tensor, x: torch.Tensor, dval: torch.Tensor) -> torch.Tensor:
+        """dval[p] = G[row(p), :] . X[col(p), :] (the values' adjoint)."""
+        _require_cuda(g, x, dval)
+        if g.dtype != torch.float64 or x.dtype != torch.float64:
+            raise TypeError("g and x must be float64")
+        if g.shape[0] != self.m or x.shape[0] != self.n or dval.dtype != self.val_dtype:
+            raise ValueError("g must be (m, k), x (n, k), dval of the values' dtype")
+        rc = _lib.load().sblas_batch_sddmm(self._h, _ptr(g), self.k, _ptr(x), self.k, _ptr(dval),
+                                           _stream_ptr(self.device))
+        _lib.check(rc)
+        return dval
+
+
+def csr_transpose(m: int, n: int, rowptr: torch.Tensor,
+                  col: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    """Device CSR structure of A^T: (t_rowptr, t_col, perm) with the values of
+    A^T equal to val[perm]."""
+    dev = _require_cuda(rowptr, col)
+    nnz = col.numel()
+    lib = _lib.load()
+    wb = int(lib.sblas_csr_transpose_workspace_bytes(m, n, nnz))
+    work = torch.empty(max(wb, 1), dtype=torch.uint8, device=dev)
+    t_rowptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    t_col = torch.empty(nnz, dtype=torch.int32, device=dev)
+    perm = torch.empty(nnz, dtype=torch.int32, device=dev)
+    with torch.cuda.device(dev):
+        rc = lib.sblas_csr_transpose(m, n, nnz, _ptr(rowptr), _ptr(col), _ptr(t_rowptr),
+                                     _ptr(t_col), _ptr(perm), _ptr(work), wb, _stream_ptr(dev))
+    _lib.check(rc)
+    return t_rowptr, t_col, perm
+
+
+def gather_values(val: torch.Tensor, perm: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
+    """out[p] = val[perm[p]] on the device (FP64 or FP32 values)."""
+    dev = _require_cuda(val, perm, out)
+    rc = _lib.load().sblas_gather_values(perm.numel(), _val_kind(val), _ptr(val), _ptr(perm),
+                                         _ptr(out), _stream_ptr(dev))
+    _lib.check(rc)
+    return out

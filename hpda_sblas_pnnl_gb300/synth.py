@@ -175,6 +175,31 @@ def banded_fem(m: int = 2_000_000, per_row: int = 140, band: int = 20_000, offba
     return CSR(m, m, rowptr, col, val), x
 
 
+def batch_uneven(nmat: int = 64, rows: tuple[int, int] = (10_000, 1_000_000),
+                 deg: tuple[float, float] = (4.0, 64.0), seed: int = 64,
+                 device="cpu") -> list[CSR]:
+    """Uneven batch: row counts log-uniform in `rows`, mean nonzeros per row
+    log-uniform in `deg`; even-numbered matrices power-law (N(0, 1) values,
+    maximum row length min(20000, m)), odd-numbered banded FEM-like (band
+    width min(20000, m)).  Square matrices, FP64 values."""
+    g = _gen(seed, "cpu")
+    lo_r, hi_r = math.log(rows[0]), math.log(rows[1])
+    lo_d, hi_d = math.log(deg[0]), math.log(deg[1])
+    out = []
+    for i in range(nmat):
+        u = torch.rand(2, generator=g, dtype=torch.float64)
+        m = int(round(math.exp(lo_r + (hi_r - lo_r) * float(u[0]))))
+        d = math.exp(lo_d + (hi_d - lo_d) * float(u[1]))
+        if i % 2 == 0:
+            a, _ = powerlaw(m=m, mean_deg=d, dmax=min(20_000, m), seed=seed * 1000 + i,
+                            device=device, values="normal")
+        else:
+            a, _ = banded_fem(m=m, per_row=max(3, int(round(d))), band=min(20_000, m),
+                              seed=seed * 1000 + i, device=device)
+        out.append(a)
+    return out
+
+
 def csr_to_coo_rows(a: CSR) -> torch.Tensor:
     """Row index of every nonzero (row-sorted COO)."""
     cnt = (a.rowptr[1:] - a.rowptr[:-1]).to(torch.int64)
@@ -201,5 +226,5 @@ def compulsory_bytes(m: int, n: int, nnz: int, val_bytes: int = 8, beta_nonzero:
     return val_bytes * nnz + idx + k * 8 * n + k * 8 * m * (2 if beta_nonzero else 1)
 
 
-__all__ = ["CSR", "zipf_rows", "powerlaw", "banded_fem", "csr_to_coo_rows", "csr_to_csc",
-           "compulsory_bytes"]
+__all__ = ["CSR", "zipf_rows", "powerlaw", "banded_fem", "batch_uneven", "csr_to_coo_rows",
+           "csr_to_csc", "compulsory_bytes"]

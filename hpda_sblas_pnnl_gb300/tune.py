@@ -1,0 +1,73 @@
+"""Autotuner: picks tile shapes by timing the compiled candidates on the
+caller's own matrices (CUDA events on the current stream, after a warm-up).
+
+  batch_s     nonzeros per lane (s) of the batched SpMM for a batch and k
+  tile_sigma  nonzeros per thread (sigma) of the single-matrix tile kernel
+
+Candidates run into scratch outputs, so the caller's Y is never written.
+Choices are cached for the process, keyed by the value kind, k and the
+shapes (m, n, nnz) of the matrices.
+"""
+from __future__ import annotations
+
+import statistics
+
+import torch
+
+from . import ops
+
+_CACHE: dict = {}
+
+
+def _time_ms(fn, reps: int) -> float:
+    stream = torch.cuda.current_stream()
+    fn()
+    ts = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def batch_s(matrices, xs, k: int, candidates=(4, 8, 16, 32), reps: int = 5):
+    """Best s for ops.BatchPlan(matrices, xs, ys, k); returns (s, {s: ms})."""
+    key = ("batch", k, tuple((rp.numel() - 1, x.shape[0], c.numel(), ops._val_kind(v))
+                             for (rp, c, v), x in zip(matrices, xs)))
+    if key in _CACHE:
+        return _CACHE[key]
+    ys = [torch.empty((rp.numel() - 1, k) if k > 1 else (rp.numel() - 1,), dtype=torch.float64,
+                      device=x.device) for (rp, _, _), x in zip(matrices, xs)]
+    times = {}
+    for s in candidates:
+        plan = ops.BatchPlan(matrices, xs, ys, k, s=s)
+        times[s] = _time_ms(plan, reps)
+        plan.close()
+    best = min(times, key=times.get)
+    _CACHE[key] = (best, times)
+    return best, times
+
+
+def tile_sigma(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
+               x: torch.Tensor, candidates=None, reps: int = 5):
+    """Best sigma for ops.CsrPlan(rowptr, col, val); returns (sigma, {sigma: ms})."""
+    m = rowptr.numel() - 1
+    key = ("tile", m, x.numel(), col.numel(), ops._val_kind(val))
+    if key in _CACHE:
+        return _CACHE[key]
+    y = torch.empty(m, dtype=torch.float64, device=x.device)
+    times = {}
+    for sg in candidates or ops.compiled_sigmas():
+        plan = ops.CsrPlan(rowptr, col, val, n=x.numel(), sigma=sg)
+        times[sg] = _time_ms(lambda: plan(x, y), reps)
+        del plan
+    best = min(times, key=times.get)
+    _CACHE[key] = (best, times)
+    return best, times
+
+
+__all__ = ["batch_s", "tile_sigma"]

@@ -152,6 +152,73 @@ SBLAS_API int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_va
 SBLAS_API int sblas_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
                              void *stream);
 
+/* ---- batched SpMM: many CSR matrices, k right-hand sides each ----------
+ * Replaces the reference's multi-chunk task pool (spMV_mgpu_v2,
+ * src/dspmv_mgpu_v2.cu:103-307, tasks include/spmv_task.h:4-36) on one GPU:
+ * every matrix of the batch is cut into units of 32*s nonzeros and one
+ * persistent kernel runs all units (then a short carry fix-up kernel).
+ *   Y_i = alpha_i * A_i * X_i + beta_i * Y_i
+ * X_i: n_i x k, row-major, row stride ldx >= k (the k values of one row
+ * contiguous); Y_i: m_i x k, row-major, row stride ldy >= k.  For k >= 2, x
+ * and y must be 16-byte aligned and ldx, ldy even.  k in {1, 2, 4, 8, 16};
+ * s in {4, 8, 16, 32} (0: the default for k). */
+typedef struct sblas_batch_matrix {
+    int m;
+    int n;
+    long long nnz;          /* < 2^31 (int32 row pointer) */
+    const void *val;        /* per val_kind; NULL for SBLAS_VAL_PATTERN */
+    const int *rowptr;      /* m + 1 entries */
+    const int *col;
+    const double *x;
+    int ldx;
+    double *y;
+    int ldy;
+    double alpha;
+    double beta;
+} sblas_batch_matrix;
+
+typedef struct sblas_batch_plan sblas_batch_plan;
+
+/* Default nonzeros per lane for k right-hand sides (0 if k not compiled). */
+SBLAS_API int sblas_batch_default_s(int k);
+/* Analysis: copies the descriptors to the device, computes the unit
+ * partition and the persistent grid.  Allocates the plan's device memory
+ * (descriptors, unit table, carries) and synchronises `stream`. */
+SBLAS_API int sblas_batch_plan_create(int nmat, const sblas_batch_matrix *mats, int k,
+                                      int val_kind, int s, void *stream,
+                                      sblas_batch_plan **plan);
+SBLAS_API int sblas_batch_plan_destroy(sblas_batch_plan *plan);
+/* units of the plan, its s, and the device bytes it holds */
+SBLAS_API int sblas_batch_plan_info(const sblas_batch_plan *plan, long long *units, int *s,
+                                    size_t *device_bytes);
+/* Runs the whole batch on `stream`: two kernel launches, no allocation, no
+ * copy, no synchronisation (can be captured in a CUDA graph). */
+SBLAS_API int sblas_batch_spmm(const sblas_batch_plan *plan, void *stream);
+/* Single-matrix plans (nmat == 1): the same run with X, Y, alpha and beta
+ * given per call (the structure and k fixed by the plan); val: values of
+ * the plan's kind replacing the plan's (same pattern), or NULL. */
+SBLAS_API int sblas_batch_spmm_xy(const sblas_batch_plan *plan, const void *val, const double *x,
+                                  int ldx, double *y, int ldy, double alpha, double beta,
+                                  void *stream);
+/* Adjoint of Y = A X with respect to the stored values, for a single-matrix
+ * plan: dval[p] = sum_c G[row(p), c] * X[col(p), c], p in CSR order.  G is
+ * m x k (row stride ldg), X n x k; dval FP64 or FP32 as the plan's values
+ * (pattern plans: SBLAS_ERR_UNSUPPORTED).  No counterpart in the reference. */
+SBLAS_API int sblas_batch_sddmm(const sblas_batch_plan *plan, const double *g, int ldg,
+                                const double *x, int ldx, void *dval, void *stream);
+
+/* Transpose of a CSR structure on the device (setup for A^T products):
+ * t_rowptr[n + 1], t_col[nnz] (the rows of A, ascending in each row of
+ * A^T) and perm[nnz]: position in A of every entry of A^T, so that the
+ * values of A^T are val[perm].  work: sblas_csr_transpose_workspace_bytes. */
+SBLAS_API size_t sblas_csr_transpose_workspace_bytes(int m, int n, long long nnz);
+SBLAS_API int sblas_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
+                                  int *t_rowptr, int *t_col, int *perm, void *work,
+                                  size_t work_bytes, void *stream);
+/* dst[p] = src[perm[p]] for nnz values of the given kind (FP64 or FP32). */
+SBLAS_API int sblas_gather_values(long long nnz, int val_kind, const void *src, const int *perm,
+                                  void *dst, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -308,3 +308,58 @@ void oracle_coo2csc(int m, int n, int nnz, const double *cooval, const int *coor
     (void)m;
     counting_sort_compress(n, nnz, coocol, coorow, cooval, csccolptr, cscrow, cscval);
 }
+
+/* Several right-hand sides: the csr_spmv_cpu loop (test/dspmv_test_smt.cu:39-52)
+ * applied to every column c of a row-major X (n x k, row stride ldx) into Y
+ * (m x k, row stride ldy), same per-row summation order.  The reference has
+ * no SpMM; its task pool (src/dspmv_mgpu_v2.cu:103-307) runs independent
+ * products, which this restates column by column.  val == NULL: every stored
+ * entry is 1 (pattern-only matrices). */
+void oracle_csr_spmm(int m, int n, int k, const double *alpha, const double *val,
+                     const int *rowptr, const int *col, const double *x, int ldx,
+                     const double *beta, double *y, int ldy, int nthreads)
+{
+    (void)n;
+    const double a = *alpha, b = *beta;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    #pragma omp parallel for schedule(static) num_threads(nthreads)
+#else
+    (void)nthreads;
+#endif
+    for (int i = 0; i < m; i++) {
+        for (int c = 0; c < k; c++) {
+            double sum = 0.0;
+            for (int j = rowptr[i]; j < rowptr[i + 1]; j++)
+                sum += (val ? val[j] : 1.0) * x[(long long)col[j] * ldx + c];
+            y[(long long)i * ldy + c] = a * sum + b * y[(long long)i * ldy + c];
+        }
+    }
+}
+
+/* Adjoint of Y = A X with respect to X (no counterpart in the reference):
+ * dX = A^T G, scattered row by row in storage order (dX overwritten). */
+void oracle_csr_spmm_t(int m, int n, int k, const double *val, const int *rowptr,
+                       const int *col, const double *g, int ldg, double *dx, int lddx)
+{
+    for (int j = 0; j < n; j++)
+        for (int c = 0; c < k; c++) dx[(long long)j * lddx + c] = 0.0;
+    for (int i = 0; i < m; i++)
+        for (int p = rowptr[i]; p < rowptr[i + 1]; p++)
+            for (int c = 0; c < k; c++)
+                dx[(long long)col[p] * lddx + c] += (val ? val[p] : 1.0) * g[(long long)i * ldg + c];
+}
+
+/* Adjoint of Y = A X with respect to the stored values (no counterpart in
+ * the reference): dval[p] = sum over c of G[row(p), c] * X[col(p), c]. */
+void oracle_csr_sddmm(int m, int k, const int *rowptr, const int *col, const double *g, int ldg,
+                      const double *x, int ldx, double *dval)
+{
+    for (int i = 0; i < m; i++)
+        for (int p = rowptr[i]; p < rowptr[i + 1]; p++) {
+            double s = 0.0;
+            for (int c = 0; c < k; c++)
+                s += g[(long long)i * ldg + c] * x[(long long)col[p] * ldx + c];
+            dval[p] = s;
+        }
+}

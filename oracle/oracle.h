@@ -42,6 +42,14 @@ void oracle_coo2csr(int m, int n, int nnz, const double *cooval, const int *coor
 void oracle_coo2csc(int m, int n, int nnz, const double *cooval, const int *coorow,
                     const int *coocol, double *cscval, int *csccolptr, int *cscrow);
 
+void oracle_csr_spmm(int m, int n, int k, const double *alpha, const double *val,
+                     const int *rowptr, const int *col, const double *x, int ldx,
+                     const double *beta, double *y, int ldy, int nthreads);
+void oracle_csr_spmm_t(int m, int n, int k, const double *val, const int *rowptr,
+                       const int *col, const double *g, int ldg, double *dx, int lddx);
+void oracle_csr_sddmm(int m, int k, const int *rowptr, const int *col, const double *g, int ldg,
+                      const double *x, int ldx, double *dval);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,12 @@ def _lib() -> C.CDLL:
         _o.oracle_gen_g.restype = C.c_longlong
         for name in ("oracle_coo2csr", "oracle_coo2csc"):
             getattr(_o, name).argtypes = [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip, _dp, _ip, _ip]
+        _o.oracle_csr_spmm.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp,
+                                       C.c_int, _dp, _dp, C.c_int, C.c_int]
+        _o.oracle_csr_spmm_t.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _ip, _ip, _dp, C.c_int,
+                                         _dp, C.c_int]
+        _o.oracle_csr_sddmm.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, _dp, C.c_int,
+                                        _dp]
     return _o
 
 
@@ -97,6 +103,48 @@ def csr_spmv(m, n, rowptr, col, val, x, y, alpha=1.0, beta=0.0, threads=0, dot2=
     else:
         _lib().oracle_csr_spmv(*args)
     return y
+
+
+def _dn(a):
+    return None if a is None else _d(a)
+
+
+def _k2(a, rows):
+    """(rows, k) C-contiguous float64 view of a 1-D or 2-D array, and k."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        a = a.reshape(rows, 1)
+    return a, a.shape[1]
+
+
+def csr_spmm(m, n, rowptr, col, val, x, y, alpha=1.0, beta=0.0, threads=0):
+    """Y = alpha*A*X + beta*Y for row-major X (n, k), Y (m, k); val None:
+    pattern.  Returns a new Y (input untouched), shaped like y."""
+    shape = np.shape(y)
+    x, k = _k2(x, n)
+    y = np.array(_k2(y, m)[0], copy=True)
+    a, b = _ab(alpha, beta)
+    _lib().oracle_csr_spmm(m, n, k, a, _dn(val), _i(rowptr), _i(col), _d(x), k, b, _d(y), k,
+                           threads)
+    return y.reshape(shape)
+
+
+def csr_spmm_t(m, n, rowptr, col, val, g):
+    """dX = A^T G for G (m, k); returns (n, k) (or (n,) for 1-D g)."""
+    g1 = np.ndim(g) == 1
+    g, k = _k2(g, m)
+    dx = np.zeros((n, k))
+    _lib().oracle_csr_spmm_t(m, n, k, _dn(val), _i(rowptr), _i(col), _d(g), k, _d(dx), k)
+    return dx[:, 0] if g1 else dx
+
+
+def csr_sddmm(m, n, rowptr, col, g, x):
+    """dval[p] = sum_c G[row(p), c] * X[col(p), c]."""
+    g, k = _k2(g, m)
+    x, _ = _k2(x, n)
+    dval = np.zeros(col.size)
+    _lib().oracle_csr_sddmm(m, k, _i(rowptr), _i(col), _d(g), k, _d(x), k, _d(dval))
+    return dval
 
 
 def coo_spmv(m, n, row, col, val, x, y, alpha=1.0, beta=0.0):

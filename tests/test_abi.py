@@ -79,6 +79,32 @@ def test_errors_are_statuses_not_exits(sblas_lib):
     np.testing.assert_array_equal(y, g["y0"])  # untouched on failure
 
 
+def test_batch_plan_argument_errors(sblas_lib):
+    """Batched-SpMM plan validation happens on the host, before any CUDA
+    call: bad counts, uncompiled k or s, null or misaligned pointers."""
+    from hpda_sblas_pnnl_gb300 import _lib
+    assert [sblas_lib.sblas_batch_default_s(k) for k in (1, 2, 4, 8, 16)] == [16, 16, 8, 8, 4]
+    assert sblas_lib.sblas_batch_default_s(3) == 0
+    plan = C.c_void_p()
+    one = (_lib.BatchMatrix * 1)()
+    one[0] = _lib.BatchMatrix(4, 4, 4, 4096, 8192, 12288, 16384, 2, 20480, 2, 1.0, 0.0)
+    assert sblas_lib.sblas_batch_plan_create(0, one, 2, 0, 0, None, C.byref(plan)) == -1
+    assert sblas_lib.sblas_batch_plan_create(1, one, 3, 0, 0, None, C.byref(plan)) == -7
+    assert sblas_lib.sblas_batch_plan_create(1, one, 2, 0, 5, None, C.byref(plan)) == -7
+    assert sblas_lib.sblas_batch_plan_create(1, one, 2, 9, 0, None, C.byref(plan)) == -1
+    bad = (_lib.BatchMatrix * 1)()
+    bad[0] = _lib.BatchMatrix(4, 4, 4, 4096, None, 12288, 16384, 2, 20480, 2, 1.0, 0.0)
+    assert sblas_lib.sblas_batch_plan_create(1, bad, 2, 0, 0, None, C.byref(plan)) == -1
+    bad[0] = _lib.BatchMatrix(4, 4, 4, 4096, 8192, 12288, 16392, 2, 20480, 2, 1.0, 0.0)
+    assert sblas_lib.sblas_batch_plan_create(1, bad, 2, 0, 0, None, C.byref(plan)) == -5
+    assert b"aligned" in sblas_lib.sblas_last_error()
+    bad[0] = _lib.BatchMatrix(4, 4, 4, 4096, 8192, 12288, 16384, 1, 20480, 2, 1.0, 0.0)
+    assert sblas_lib.sblas_batch_plan_create(1, bad, 2, 0, 0, None, C.byref(plan)) == -5
+    assert plan.value is None
+    assert sblas_lib.sblas_batch_spmm(None, None) == -1
+    assert sblas_lib.sblas_batch_plan_destroy(None) == 0
+
+
 def test_compat_switch_and_shapes(sblas_lib):
     sblas_lib.sblas_set_compat_mode(1)
     assert sblas_lib.sblas_get_compat_mode() == 1

@@ -127,3 +127,30 @@ def test_oracle_equals_reference_binary_on_random_inputs():
                                       O.ref_coo_spmv(m, n, row, col, val, x, y0, a, b))
         for idx in range(0, int(rowptr[-1]), 7):
             assert O.get_row_from_index(m, rowptr, idx) == O.ref_get_row_from_index(m, rowptr, idx)
+
+
+def test_oracle_spmm_and_adjoints_match_scipy():
+    """The multi-right-hand-side and adjoint restatements (oracle_csr_spmm,
+    oracle_csr_spmm_t, oracle_csr_sddmm) against scipy.sparse."""
+    sp = pytest.importorskip("scipy.sparse")
+    rng = np.random.default_rng(4)
+    a = sp.random(300, 200, density=0.05, format="csr", random_state=4)
+    rp, c, v = a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data
+    for k in (1, 3, 8):
+        x = rng.standard_normal((200, k))
+        y0 = rng.standard_normal((300, k))
+        y = O.csr_spmm(300, 200, rp, c, v, x, y0, -1.5, 0.25)
+        np.testing.assert_allclose(y, -1.5 * (a @ x) + 0.25 * y0, rtol=1e-13, atol=1e-13)
+        ypat = O.csr_spmm(300, 200, rp, c, None, x, y0, 1.0, 0.0)
+        np.testing.assert_allclose(ypat, (a != 0).astype(np.float64) @ x, rtol=1e-13, atol=1e-13)
+        g = rng.standard_normal((300, k))
+        np.testing.assert_allclose(O.csr_spmm_t(300, 200, rp, c, v, g), a.T @ g, rtol=1e-13,
+                                   atol=1e-13)
+        rows = np.repeat(np.arange(300), np.diff(rp))
+        np.testing.assert_allclose(O.csr_sddmm(300, 200, rp, c, g, x),
+                                   np.einsum("pk,pk->p", g[rows], x[c]), rtol=1e-13, atol=1e-13)
+    # one right-hand side as a 1-D vector is the plain SpMV loop, bit for bit
+    x1 = rng.standard_normal(200)
+    y1 = rng.standard_normal(300)
+    np.testing.assert_array_equal(O.csr_spmm(300, 200, rp, c, v, x1, y1, 2.0, 0.5),
+                                  O.csr_spmv(300, 200, rp, c, v, x1, y1, 2.0, 0.5))
