@@ -509,9 +509,18 @@ __global__ void __launch_bounds__(CTA) batch_sddmm_kernel(const Args a)
             double gr[K], xr[K];
             gather_row<K>(a.g, r, a.ldg, gr, pol);
             gather_row<K>(a.x, __ldcs(col + p), a.ldx, xr, pol);
-            double d = 0.0;
+            // four independent partial sums (the dependent DFMA latency is
+            // long on this GPU), joined at the end
+            constexpr int NP = K >= 4 ? 4 : K;
+            double part[NP];
 #pragma unroll
-            for (int c = 0; c < K; ++c) d = fma(gr[c], xr[c], d);
+            for (int q = 0; q < NP; ++q) part[q] = 0.0;
+#pragma unroll
+            for (int c = 0; c < K; ++c) part[c % NP] = fma(gr[c], xr[c], part[c % NP]);
+            double d;
+            if constexpr (NP == 4) d = (part[0] + part[1]) + (part[2] + part[3]);
+            else if constexpr (NP == 2) d = part[0] + part[1];
+            else d = part[0];
             if constexpr (VK == VAL_F32) static_cast<float *>(a.dval)[p] = (float)d;
             else static_cast<double *>(a.dval)[p] = d;
         }

@@ -572,7 +572,6 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
         ptx::fence_mbar_init();
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
-    if (VK != VAL_F64)
     for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
     __syncthreads();
     if (warp == NCW)
