@@ -1,10 +1,10 @@
 """Benchmark of the FP64 SpMV hot path on GB300 (one JSON line on stdout).
 
 Workload (the power-law configuration): y = 1.0*A*x + 0.0*y, A a 4.0M x 4.0M
-power-law graph with ~70M nonzeros (out-degree exponent 2.1, max row 20k),
+power-law graph with 64.2M nonzeros (out-degree exponent 2.1, max row 20k),
 values 1.0 FP64, x ~ U(0,1), int32 CSR indices.  One step = one SpMV over
 the whole matrix through sblas_dcsrmv (tile partition + tile kernel + carry
-fix-up; 3 launches), inputs resident in HBM.  The compulsory bytes (920 MB:
+fix-up; 3 launches), inputs resident in HBM.  The compulsory bytes (851 MB:
 val, col, rowptr, x read once, y written once) exceed the 129 MB L2, so no
 flush is needed between steps; x (32 MB) stays L2-resident by design.
 
@@ -35,7 +35,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "SpMV HBM GB/s & % roofline: plain FP64 vs mixed/batched/fwd+bwd at stated err"
-WORKLOAD = ("power-law graph 4.0M x 4.0M, ~70M nnz (exponent 2.1, max row 20k), values 1.0 "
+WORKLOAD = ("power-law graph 4.0M x 4.0M, 64.2M nnz (exponent 2.1, max row 20k), values 1.0 "
             "FP64, x~U(0,1); FP64 CSR y=1.0*A*x+0.0*y")
 FALLBACK_HBM = 6800.0
 
@@ -222,7 +222,16 @@ def run_ours(args):
     y = torch.zeros(m, dtype=torch.float64, device=dev)
     bytes_step = synth.compulsory_bytes(m, n, nnz)
     kernel = ops.KERNEL_MERGEPATH
-    sigma = args.sigma if args.sigma > 0 else ops.default_sigma(m, nnz)
+    # tile shape: --sigma, else the library default for --kernel-only (the
+    # profiling case), else the autotuner's measured pick on this matrix
+    sigma_times = None
+    if args.sigma > 0:
+        sigma = args.sigma
+    elif args.kernel_only:
+        sigma = ops.default_sigma(m, nnz)
+    else:
+        from hpda_sblas_pnnl_gb300 import tune
+        sigma, sigma_times = tune.tile_sigma(a.rowptr, a.col, a.val, x)
     work = torch.empty(ops.workspace_bytes(nnz, sigma), dtype=torch.uint8, device=dev)
 
     def step():
@@ -283,8 +292,11 @@ def run_ours(args):
                 "frac": round(achieved / pk, 4), "traffic": None, "peak_source": pk_kind,
                 "kernel": f"tile_spmv_kernel<128,{sigma},F64> + tile_fixup_kernel",
                 "kernel_us": round(k_ms * 1e3, 2),
-                "fp64_note": "FP64 pipe measured at 5.04e11 DFMA/s; 1 DFMA per nonzero "
-                             f"caps this matrix at {5.04e11 * bytes_step / nnz / 1e9:.0f} GB/s"}
+                "bounds_note": "1 DFMA per nonzero at the measured 5.3e11 DFMA/s caps this matrix "
+                               f"at {5.3e11 * bytes_step / nnz / 1e9:.0f} GB/s; one random L2 "
+                               "gather per nonzero at the measured 2.8e11/s caps it at "
+                               f"{2.8e11 * bytes_step / nnz / 1e9:.0f} GB/s "
+                               "(profiles/probes_gb300.md)"}
         traffic_file = ROOT / "profiles" / "traffic.json"
         if traffic_file.exists():
             try:
@@ -342,7 +354,9 @@ def run_ours(args):
             "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
             "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
                        "bytes_per_step": bytes_step, "kernel": "2 (nnz tiles)", "sigma": sigma,
-                       "l2": "inputs larger than L2 (920 MB > 129 MB), no flush",
+                       "sigma_tuner_ms": ({str(k): round(v, 4) for k, v in sigma_times.items()}
+                                          if sigma_times else None),
+                       "l2": f"inputs larger than L2 ({bytes_step / 1e6:.0f} MB > 129 MB), no flush",
                        "launches": "tile partition + tile kernel + carry fix-up",
                        "check_rel_err": chk, "e2e_max_abs_diff": e2e_err},
             "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
@@ -391,7 +405,7 @@ def run_extras(dev, stream, args):
 def run_banded_extra(dev, stream, args, timed, threads, pk):
     import numpy as np
     import torch
-    from hpda_sblas_pnnl_gb300 import ops, synth
+    from hpda_sblas_pnnl_gb300 import ops, synth, tune
     from oracle import oracle as O
     res = {}
     a, x = synth.banded_fem(device=dev)
@@ -401,12 +415,14 @@ def run_banded_extra(dev, stream, args, timed, threads, pk):
     nref = np.linalg.norm(ref)
     y = torch.zeros(m, dtype=torch.float64, device=dev)
     for name, val, vb in (("banded_fp64", a.val, 8), ("banded_fp32val", a.val.float(), 4)):
-        plan = ops.CsrPlan(a.rowptr, a.col, val)
+        sg, _ = tune.tile_sigma(a.rowptr, a.col, val, x)
+        plan = ops.CsrPlan(a.rowptr, a.col, val, sigma=sg)
         ms = timed(plan, x, y)
         err = float(np.linalg.norm(y.cpu().numpy() - ref) / nref)
         b = synth.compulsory_bytes(m, n, nnz, val_bytes=vb)
         res[name] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
-                     "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err, "nnz": nnz}
+                     "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err, "nnz": nnz,
+                     "sigma": sg}
         del plan
     if "banded_fp64" in res and "banded_fp32val" in res:
         res["fp32val_speedup"] = round(res["banded_fp64"]["us"] / res["banded_fp32val"]["us"], 3)
@@ -418,19 +434,21 @@ def run_banded_extra(dev, stream, args, timed, threads, pk):
 def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
     import numpy as np
     import torch
-    from hpda_sblas_pnnl_gb300 import ops, synth
+    from hpda_sblas_pnnl_gb300 import ops, synth, tune
     from oracle import oracle as O
     res = {}
     a, x = synth.powerlaw(seed=args.seed, device=dev)
     y = torch.zeros(a.m, dtype=torch.float64, device=dev)
-    plan = ops.CsrPlan(a.rowptr, a.col, None)
+    sg, _ = tune.tile_sigma(a.rowptr, a.col, None, x)
+    plan = ops.CsrPlan(a.rowptr, a.col, None, sigma=sg)
     ms = timed(plan, x, y)
     b = synth.compulsory_bytes(a.m, a.n, a.nnz, val_bytes=0)
     rp, c, v = a.numpy()
     ref = O.csr_spmv(a.m, a.n, rp, c, v, x.cpu().numpy(), np.zeros(a.m), threads=threads)
     err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
     res["powerlaw_pattern"] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
-                               "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err}
+                               "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err,
+                               "sigma": sg}
     # CSC and COO (device conversion once, then the tile kernel; conversion timed apart)
     colptr, rowidx, cval = synth.csr_to_csc(a)
     torch.cuda.synchronize()
@@ -542,7 +560,7 @@ def run_autograd_extra(dev, stream, args):
     gy = torch.randn((a.m, k), generator=g, dtype=torch.float64, device=dev)
     res = {"m": a.m, "nnz": a.nnz, "k": k}
     for name, dtype in (("fp64", torch.float64), ("fp32val", torch.float32)):
-        op = autograd.CsrOperator(a.rowptr, a.col, a.n, k, value_dtype=dtype)
+        op = autograd.CsrOperator(a.rowptr, a.col, a.n, k, value_dtype=dtype, s=None)
         val = a.val.to(dtype).requires_grad_(True)
         x = x0.clone().requires_grad_(True)
         y = torch.empty((a.m, k), dtype=torch.float64, device=dev)
@@ -560,12 +578,17 @@ def run_autograd_extra(dev, stream, args):
             fwd_bwd()
         f_ms = statistics.median(cuda_event_ms(fwd, stream, 10))
         fb_ms = statistics.median(cuda_event_ms(fwd_bwd, stream, 10))
+        # the backward's parts alone: dX = A^T G (with the value permutation), dval
+        dx_ms = statistics.median(cuda_event_ms(lambda: op.grad_x(val.detach(), gy), stream, 10))
+        dv_ms = statistics.median(cuda_event_ms(lambda: op.grad_val(gy, x.detach()), stream, 10))
         vb = 8 if dtype == torch.float64 else 4
         fbytes = synth.compulsory_bytes(a.m, a.n, a.nnz, val_bytes=vb, k=k)
         res[name] = {"fwd_ms": round(f_ms, 3), "fwd_bwd_ms": round(fb_ms, 3),
                      "ratio": round(fb_ms / f_ms, 3),
                      "fwd_fp64_tflops": round(2.0 * a.nnz * k / f_ms / 1e9, 4),
-                     "fwd_gbs": round(fbytes / f_ms / 1e6, 1)}
+                     "fwd_gbs": round(fbytes / f_ms / 1e6, 1),
+                     "s_fwd": op.fwd.s, "s_bwd": op.bwd.s, "dx_ms": round(dx_ms, 3),
+                     "dval_ms": round(dv_ms, 3)}
         del op, val, x, y
         torch.cuda.empty_cache()
     return res

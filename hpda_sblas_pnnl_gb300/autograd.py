@@ -17,17 +17,19 @@ from __future__ import annotations
 
 import torch
 
-from . import ops
+from . import ops, tune
 
 
 class CsrOperator:
     """A CSR pattern (int32 rowptr, col) of an m x n matrix, prepared for
     differentiable products with k right-hand sides (k in 1, 2, 4, 8, 16).
     value_dtype: torch.float64, torch.float32, or None for a pattern-only
-    matrix (every stored entry 1, nothing to differentiate but X)."""
+    matrix (every stored entry 1, nothing to differentiate but X).
+    s: nonzeros per lane of the forward and transposed plans; None picks
+    each by measurement (tune.spmm_s), 0 takes the library default."""
 
     def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, n: int, k: int,
-                 value_dtype: torch.dtype | None = torch.float64, s: int = 0):
+                 value_dtype: torch.dtype | None = torch.float64, s: int | None = 0):
         self.m = rowptr.numel() - 1
         self.n = int(n)
         self.k = int(k)
@@ -37,10 +39,14 @@ class CsrOperator:
         proto = None if value_dtype is None else torch.zeros(self.nnz, dtype=value_dtype,
                                                                device=dev)
         self.rowptr, self.col = rowptr, col
-        self.fwd = ops.SpmmPlan(rowptr, col, proto, n=self.n, k=self.k, s=s)
         self.t_rowptr, self.t_col, self.perm = ops.csr_transpose(self.m, self.n, rowptr, col)
         self.val_t = None if proto is None else torch.empty_like(proto)
-        self.bwd = ops.SpmmPlan(self.t_rowptr, self.t_col, self.val_t, n=self.m, k=self.k, s=s)
+        s_f = s_b = s
+        if s is None:
+            s_f, _ = tune.spmm_s(rowptr, col, proto, self.n, self.k)
+            s_b, _ = tune.spmm_s(self.t_rowptr, self.t_col, self.val_t, self.m, self.k)
+        self.fwd = ops.SpmmPlan(rowptr, col, proto, n=self.n, k=self.k, s=s_f)
+        self.bwd = ops.SpmmPlan(self.t_rowptr, self.t_col, self.val_t, n=self.m, k=self.k, s=s_b)
 
     def _shape(self, rows: int, like: torch.Tensor) -> tuple:
         return (rows,) if like.dim() == 1 else (rows, self.k)

@@ -2,6 +2,7 @@
 caller's own matrices (CUDA events on the current stream, after a warm-up).
 
   batch_s     nonzeros per lane (s) of the batched SpMM for a batch and k
+  spmm_s      the same for one matrix with k right-hand sides (ops.SpmmPlan)
   tile_sigma  nonzeros per thread (sigma) of the single-matrix tile kernel
 
 Candidates run into scratch outputs, so the caller's Y is never written.
@@ -52,6 +53,28 @@ def batch_s(matrices, xs, k: int, candidates=(4, 8, 16, 32), reps: int = 5):
     return best, times
 
 
+def spmm_s(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, n: int, k: int,
+           candidates=(4, 8, 16, 32), reps: int = 5):
+    """Best s for ops.SpmmPlan(rowptr, col, val, n, k); returns (s, {s: ms}).
+    Times Y = A X on a scratch X of ones (the schedule does not depend on
+    the values of X)."""
+    m = rowptr.numel() - 1
+    key = ("spmm", m, n, col.numel(), ops._val_kind(val), k)
+    if key in _CACHE:
+        return _CACHE[key]
+    dev = rowptr.device
+    x = torch.ones((n, k) if k > 1 else (n,), dtype=torch.float64, device=dev)
+    y = torch.empty((m, k) if k > 1 else (m,), dtype=torch.float64, device=dev)
+    times = {}
+    for s in candidates:
+        plan = ops.SpmmPlan(rowptr, col, val, n=n, k=k, s=s)
+        times[s] = _time_ms(lambda: plan(x, y), reps)
+        plan.close()
+    best = min(times, key=times.get)
+    _CACHE[key] = (best, times)
+    return best, times
+
+
 def tile_sigma(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
                x: torch.Tensor, candidates=None, reps: int = 5):
     """Best sigma for ops.CsrPlan(rowptr, col, val); returns (sigma, {sigma: ms})."""
@@ -70,4 +93,4 @@ def tile_sigma(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None
     return best, times
 
 
-__all__ = ["batch_s", "tile_sigma"]
+__all__ = ["batch_s", "spmm_s", "tile_sigma"]
