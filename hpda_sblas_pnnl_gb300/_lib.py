@@ -48,6 +48,8 @@ class BatchMatrix(C.Structure):
         ("ldy", C.c_int),
         ("alpha", C.c_double),
         ("beta", C.c_double),
+        ("row_ids", C.c_void_p),
+        ("val_perm", C.c_void_p),
     ]
 
 
@@ -101,6 +103,7 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_csr_transpose": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp,
                                       _vp, C.c_size_t, _vp]),
     "sblas_gather_values": (C.c_int, [C.c_longlong, C.c_int, _vp, _vp, _vp, _vp]),
+    "sblas_zero": (C.c_int, [_vp, C.c_size_t, _vp]),
     # include/spmv_kernel.h (reference signatures)
     "csr5_kernel": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _vp, _vp, _vp, _dp, _vp, _vp]),
     "spMV_mgpu_baseline": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,

@@ -2,12 +2,15 @@
 the C ABI, with hand-written adjoint kernels.
 
     forward   Y = A X                       sblas_batch_spmm_xy (A's plan)
-    backward  dX = A^T G                    sblas_batch_spmm_xy (A^T's plan, values
-                                            permuted by sblas_gather_values)
+    backward  dX = A^T G                    sblas_batch_spmm_xy (A^T's plan: rows
+                                            without entries left out, values read
+                                            through the transpose permutation)
               dval[p] = G[row(p)] . X[col(p)]  sblas_batch_sddmm (A's plan)
 
 A^T's structure (row pointer, columns and the value permutation) is built
-once on the device by sblas_csr_transpose when the operator is created.
+once on the device by sblas_csr_transpose when the operator is created; its
+empty rows are compacted away (the plan lists the rows it writes, the others
+of dX are zeroed).
 The reference has no differentiable form; the forward is its SpMV
 (test/dspmv_test_smt.cu:39-52 is the arithmetic) with k right-hand sides.
 Values are FP64 or FP32 (dval then rounded to FP32); products and sums are
@@ -40,13 +43,23 @@ class CsrOperator:
                                                                device=dev)
         self.rowptr, self.col = rowptr, col
         self.t_rowptr, self.t_col, self.perm = ops.csr_transpose(self.m, self.n, rowptr, col)
-        self.val_t = None if proto is None else torch.empty_like(proto)
+        # A^T without its empty rows (columns of A that hold no entry): the
+        # transposed plan writes only the listed rows of dX, the rest are
+        # zeroed first (setup-time compaction of the row pointer)
+        nonempty = (self.t_rowptr[1:] > self.t_rowptr[:-1]).nonzero().flatten()
+        self.t_rows = nonempty.to(torch.int32)
+        self.t_rowptr_c = torch.cat([self.t_rowptr[nonempty],
+                                     self.t_rowptr[-1:]]).to(torch.int32).contiguous()
+        # A^T's values are read through the permutation: val[perm[q]]
+        vperm = None if proto is None else self.perm
         s_f = s_b = s
         if s is None:
             s_f, _ = tune.spmm_s(rowptr, col, proto, self.n, self.k)
-            s_b, _ = tune.spmm_s(self.t_rowptr, self.t_col, self.val_t, self.m, self.k)
+            s_b, _ = tune.spmm_s(self.t_rowptr_c, self.t_col, proto, self.m, self.k,
+                                 row_ids=self.t_rows, m_out=self.n, val_perm=vperm)
         self.fwd = ops.SpmmPlan(rowptr, col, proto, n=self.n, k=self.k, s=s_f)
-        self.bwd = ops.SpmmPlan(self.t_rowptr, self.t_col, self.val_t, n=self.m, k=self.k, s=s_b)
+        self.bwd = ops.SpmmPlan(self.t_rowptr_c, self.t_col, proto, n=self.m, k=self.k,
+                                s=s_b, row_ids=self.t_rows, m_out=self.n, val_perm=vperm)
 
     def _shape(self, rows: int, like: torch.Tensor) -> tuple:
         return (rows,) if like.dim() == 1 else (rows, self.k)
@@ -56,10 +69,8 @@ class CsrOperator:
         return self.fwd(x.contiguous(), y, val=val)
 
     def grad_x(self, val: torch.Tensor | None, g: torch.Tensor) -> torch.Tensor:
-        dx = torch.empty(self._shape(self.n, g), dtype=torch.float64, device=g.device)
-        if val is not None:
-            ops.gather_values(val, self.perm, self.val_t)
-        return self.bwd(g.contiguous(), dx, val=self.val_t if val is not None else None)
+        dx = ops.zero_(torch.empty(self._shape(self.n, g), dtype=torch.float64, device=g.device))
+        return self.bwd(g.contiguous(), dx, val=val)
 
     def grad_val(self, g: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
         dval = torch.empty(self.nnz, dtype=self.value_dtype, device=g.device)

@@ -287,6 +287,18 @@ int sblas_gather_values(long long nnz, int val_kind, const void *src, const int 
     return launch_gather_values(nnz, val_kind, src, perm, dst, static_cast<cudaStream_t>(stream));
 }
 
+int sblas_zero(void *p, size_t bytes, void *stream)
+{
+    clear_error();
+    if (bytes == 0) return SBLAS_OK;
+    if (p == nullptr) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    SBLAS_CUDA_TRY(cudaMemsetAsync(p, 0, bytes, static_cast<cudaStream_t>(stream)));
+    return SBLAS_OK;
+}
+
 int sblas_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
                              void *stream)
 {

@@ -133,7 +133,7 @@ int sblas_batch_plan_create(int nmat, const sblas_batch_matrix *mats, int k, int
             set_error(SBLAS_ERR_ARG, "matrix %d: bad sizes m=%d n=%d nnz=%lld", i, q.m, q.n, q.nnz);
             return SBLAS_ERR_ARG;
         }
-        if (q.rowptr == nullptr || (q.m > 0 && q.y == nullptr) ||
+        if (q.rowptr == nullptr || ((q.m > 0 || q.row_ids) && q.y == nullptr) ||
             (q.nnz > 0 && (q.col == nullptr || q.x == nullptr ||
                            (val_kind != SBLAS_VAL_PATTERN && q.val == nullptr)))) {
             set_error(SBLAS_ERR_ARG, "matrix %d: null device pointer", i);
@@ -159,6 +159,8 @@ int sblas_batch_plan_create(int nmat, const sblas_batch_matrix *mats, int k, int
         d.ldy = q.ldy;
         d.alpha = q.alpha;
         d.beta = q.beta;
+        d.row_ids = q.row_ids;
+        d.val_perm = q.val_perm;
         const long long nu = q.nnz > 0 ? (q.nnz + unit - 1) / unit : 1;
         d.unit0 = (int)units;
         d.nunits = (int)nu;

@@ -53,7 +53,15 @@ struct Mat {
     double beta;
     int unit0;    // first unit of this matrix
     int nunits;   // units of this matrix (>= 1, also for nnz == 0)
+    const int *row_ids;   // stored row r is row row_ids[r] of Y (nullptr: r)
+    const int *val_perm;  // stored entry p has value val[val_perm[p]] (nullptr: val[p])
 };
+
+// row of Y that stored row r of a matrix writes
+__device__ __forceinline__ long long out_row(const Mat *M, int r)
+{
+    return M->row_ids ? (long long)__ldg(M->row_ids + r) : (long long)r;
+}
 
 struct Args {
     const Mat *mats;
@@ -84,7 +92,7 @@ struct Args {
 template <int K, int S>
 struct Shape {
     static constexpr int UNIT = 32 * S;                        // nonzeros per unit
-    static constexpr int RCAP = (8 * S < 1024 / K) ? 8 * S : 1024 / K;  // rows in the buffer
+    static constexpr int RCAP = (8 * S < 2048 / K) ? 8 * S : 2048 / K;  // rows in the buffer
     static constexpr int RPN = RCAP + 2;                       // row-pointer slice entries
 };
 
@@ -225,8 +233,13 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         // ---- stage the unit (coalesced), zero the row buffer ------------
         __syncwarp();
         for (int i = lane; i < cntu; i += 32) scol[i] = __ldcs(col + U0 + i);
-        if constexpr (VK != VAL_PATTERN)
-            for (int i = lane; i < cntu; i += 32) sval[i] = __ldcs(static_cast<const T *>(val) + U0 + i);
+        if constexpr (VK != VAL_PATTERN) {
+            const T *vp = static_cast<const T *>(val);
+            if (M->val_perm)
+                for (int i = lane; i < cntu; i += 32) sval[i] = __ldg(vp + __ldcs(M->val_perm + U0 + i));
+            else
+                for (int i = lane; i < cntu; i += 32) sval[i] = __ldcs(vp + U0 + i);
+        }
         if (fits) {
             for (int i = lane; i <= rp_hi - RA; i += 32) srp[i] = __ldg(rowptr + RA + i);
             for (int i = lane; i < nrows * K; i += 32) rbuf[i] = 0.0;
@@ -335,7 +348,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                 } else if (fits) {
                     store_row<K>(rbuf + (row - RA) * K, acc);
                 } else {
-                    double *yr = y + (long long)row * ldy;
+                    double *yr = y + out_row(M, row) * ldy;
 #pragma unroll
                     for (int c = 0; c < K; ++c) yr[c] = finish(acc[c], alpha, beta, yr + c);
                 }
@@ -405,7 +418,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             } else if (fits) {
                 store_row<K>(rbuf + (hrow - RA) * K, tot);
             } else {
-                double *yr = y + (long long)hrow * ldy;
+                double *yr = y + out_row(M, hrow) * ldy;
 #pragma unroll
                 for (int c = 0; c < K; ++c) yr[c] = finish(tot[c], alpha, beta, yr + c);
             }
@@ -430,13 +443,13 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             const int ne = (RB - E0) * K;
             for (int i = lane; i < ne; i += 32) {
                 const int rr = i / K, c = i - rr * K;
-                double *yp = y + (long long)(E0 + rr) * ldy + c;
+                double *yp = y + out_row(M, E0 + rr) * ldy + c;
                 *yp = finish(rbuf[(E0 - RA + rr) * K + c], alpha, beta, yp);
             }
         } else {
             for (int r = E0 + lane; r < RB; r += 32)
                 if (__ldg(rowptr + r) == __ldg(rowptr + r + 1)) {
-                    double *yr = y + (long long)r * ldy;
+                    double *yr = y + out_row(M, r) * ldy;
 #pragma unroll
                     for (int c = 0; c < K; ++c) yr[c] = finish(0.0, alpha, beta, yr + c);
                 }
@@ -451,25 +464,66 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
 template <int K>
 __global__ void batch_fixup_kernel(const Args a)
 {
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.nunits;
-         u += gridDim.x * blockDim.x) {
-        const int R = a.head_row[u];
-        if (R < 0) continue;
-        const Mat *M = a.mats + __ldg(a.unit_mat + u);
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    // whole warps iterate together (the cooperative path below needs them)
+    for (int base = blockIdx.x * blockDim.x; base < a.nunits; base += gridDim.x * blockDim.x) {
+        const int u = base + threadIdx.x;
+        int R = (u < a.nunits) ? a.head_row[u] : -1;
+        const Mat *M = (R >= 0) ? a.mats + __ldg(a.unit_mat + u) : nullptr;
+        // a row spanning 32 or more earlier units (its units are contiguous,
+        // so the unit 32 back carries the same row) is summed by the whole
+        // warp; shorter runs by their own thread, nearest unit first
+        const bool longrun = R >= 0 && u - 32 >= M->unit0 && a.tail_row[u - 32] == R;
         double t[K];
+        if (R >= 0 && !longrun) {
 #pragma unroll
-        for (int c = 0; c < K; ++c) t[c] = a.head_val[(long long)u * K + c];
-        for (int v = u - 1; v >= M->unit0 && a.tail_row[v] == R; --v) {
+            for (int c = 0; c < K; ++c) t[c] = a.head_val[(long long)u * K + c];
+            for (int v = u - 1; v >= M->unit0 && a.tail_row[v] == R; --v) {
 #pragma unroll
-            for (int c = 0; c < K; ++c) t[c] += a.tail_val[(long long)v * K + c];
+                for (int c = 0; c < K; ++c) t[c] += a.tail_val[(long long)v * K + c];
+            }
         }
-        double *y = a.override_xy ? a.y : M->y;
-        const int ldy = a.override_xy ? a.ldy : M->ldy;
-        const double alpha = a.override_xy ? a.alpha : M->alpha;
-        const double beta = a.override_xy ? a.beta : M->beta;
-        double *yr = y + (long long)R * ldy;
+        unsigned pend = __ballot_sync(FULL, longrun);
+        while (pend) {
+            const int src = __ffs(pend) - 1;
+            pend &= pend - 1;
+            const int uu = __shfl_sync(FULL, u, src);
+            const int RR = __shfl_sync(FULL, R, src);
+            const int u0 = __shfl_sync(FULL, M ? M->unit0 : 0, src);
+            // lane l sums units uu-1-l, uu-33-l, ... of the run
+            double p[K];
 #pragma unroll
-        for (int c = 0; c < K; ++c) yr[c] = finish(t[c], alpha, beta, yr + c);
+            for (int c = 0; c < K; ++c) p[c] = 0.0;
+            for (int top = uu - 1;; top -= 32) {
+                const int v = top - lane;
+                const bool in = v >= u0 && a.tail_row[v] == RR;
+                if (in) {
+#pragma unroll
+                    for (int c = 0; c < K; ++c) p[c] += a.tail_val[(long long)v * K + c];
+                }
+                if (__ballot_sync(FULL, in) != FULL) break;
+            }
+            // fixed butterfly: the same order on every run
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+#pragma unroll
+                for (int c = 0; c < K; ++c) p[c] += __shfl_xor_sync(FULL, p[c], d);
+            }
+            if (lane == src) {
+#pragma unroll
+                for (int c = 0; c < K; ++c) t[c] = a.head_val[(long long)u * K + c] + p[c];
+            }
+        }
+        if (R >= 0) {
+            double *y = a.override_xy ? a.y : M->y;
+            const int ldy = a.override_xy ? a.ldy : M->ldy;
+            const double alpha = a.override_xy ? a.alpha : M->alpha;
+            const double beta = a.override_xy ? a.beta : M->beta;
+            double *yr = y + out_row(M, R) * ldy;
+#pragma unroll
+            for (int c = 0; c < K; ++c) yr[c] = finish(t[c], alpha, beta, yr + c);
+        }
     }
 }
 
@@ -507,7 +561,7 @@ __global__ void __launch_bounds__(CTA) batch_sddmm_kernel(const Args a)
                 next = __ldg(rowptr + r + 1);
             }
             double gr[K], xr[K];
-            gather_row<K>(a.g, r, a.ldg, gr, pol);
+            gather_row<K>(a.g, out_row(M, r), a.ldg, gr, pol);
             gather_row<K>(a.x, __ldcs(col + p), a.ldx, xr, pol);
             // four independent partial sums (the dependent DFMA latency is
             // long on this GPU), joined at the end

@@ -207,7 +207,10 @@ class BatchPlan:
 
     matrices: list of (rowptr, col, val) with int32 indices and val float64,
     float32 or None (pattern; every matrix of a batch has the same value
-    kind).  xs[i]: float64 (n_i, k) row-major (or (n_i,) for k = 1);
+    kind), or (rowptr, col, val, row_ids[, val_perm]): stored row r is row
+    row_ids[r] of Y (int32, ascending; None: r) and unlisted rows of Y are
+    left untouched; stored entry p has value val[val_perm[p]] (int32; None:
+    val[p]).  xs[i]: float64 (n_i, k) row-major (or (n_i,) for k = 1);
     ys[i]: float64 (m_i, k).  The plan (sblas_batch_plan_create) copies the
     descriptors to the device and partitions all matrices into units of
     32*s nonzeros; each call is one persistent kernel plus the carry fix-up
@@ -221,7 +224,8 @@ class BatchPlan:
             raise ValueError("need one x and one y per matrix")
         flat = [t for mat in matrices for t in mat] + list(xs) + list(ys)
         dev = _require_cuda(*flat)
-        kinds = {_val_kind(v) for _, _, v in matrices}
+        matrices = [tuple(mat) + (None,) * (5 - len(mat)) for mat in matrices]
+        kinds = {_val_kind(mat[2]) for mat in matrices}
         if len(kinds) != 1:
             raise TypeError("all matrices of a batch have the same value kind")
         self.vk = kinds.pop()
@@ -229,19 +233,25 @@ class BatchPlan:
         self.device = dev
         self.matrices, self.xs, self.ys = list(matrices), list(xs), list(ys)
         arr = (_lib.BatchMatrix * len(matrices))()
-        for i, ((rp, col, val), x, y) in enumerate(zip(matrices, xs, ys)):
+        for i, ((rp, col, val, rid, vperm), x, y) in enumerate(zip(matrices, xs, ys)):
             if rp.dtype != torch.int32 or col.dtype != torch.int32:
                 raise TypeError("rowptr and col must be int32")
             if x.dtype != torch.float64 or y.dtype != torch.float64:
                 raise TypeError("x and y must be float64")
             m = rp.numel() - 1
             n = x.shape[0]
-            if y.shape[0] != m or (x.dim() > 1 and x.shape[1] != self.k) or \
+            if rid is not None and (rid.dtype != torch.int32 or rid.numel() != m):
+                raise ValueError(f"matrix {i}: row_ids must be int32 with one entry per row")
+            if vperm is not None and (vperm.dtype != torch.int32 or vperm.numel() != col.numel()):
+                raise ValueError(f"matrix {i}: val_perm must be int32 with one entry per nonzero")
+            if (y.shape[0] != m if rid is None else y.shape[0] < m) or \
+                    (x.dim() > 1 and x.shape[1] != self.k) or \
                     (y.dim() > 1 and y.shape[1] != self.k) or (self.k > 1 and x.dim() != 2):
                 raise ValueError(f"matrix {i}: x must be (n, k) and y (m, k)")
             arr[i] = _lib.BatchMatrix(m, n, col.numel(), _ptr(val).value, _ptr(rp).value,
                                       _ptr(col).value, _ptr(x).value, self.k, _ptr(y).value,
-                                      self.k, float(alpha), float(beta))
+                                      self.k, float(alpha), float(beta), _ptr(rid).value,
+                                      _ptr(vperm).value)
         lib = _lib.load()
         h = C.c_void_p()
         with torch.cuda.device(dev):
@@ -276,13 +286,14 @@ class SpmmPlan(BatchPlan):
     dtype as at construction)."""
 
     def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
-                 n: int, k: int, s: int = 0):
-        dev = _require_cuda(rowptr, col, val)
-        m = rowptr.numel() - 1
+                 n: int, k: int, s: int = 0, row_ids: torch.Tensor | None = None,
+                 m_out: int | None = None, val_perm: torch.Tensor | None = None):
+        dev = _require_cuda(rowptr, col, val, row_ids, val_perm)
+        m = rowptr.numel() - 1 if m_out is None else int(m_out)
         # placeholders fixing the shapes; every call passes its own X and Y
         xs = torch.empty((max(n, 1), k), dtype=torch.float64, device=dev)
         ys = torch.empty((max(m, 1), k), dtype=torch.float64, device=dev)
-        super().__init__([(rowptr, col, val)], [xs[:n]], [ys[:m]], k, s=s)
+        super().__init__([(rowptr, col, val, row_ids, val_perm)], [xs[:n]], [ys[:m]], k, s=s)
         self.m, self.n = m, n
         self.val_dtype = None if val is None else val.dtype
 
@@ -320,6 +331,14 @@ class SpmmPlan(BatchPlan):
                                            _stream_ptr(self.device))
         _lib.check(rc)
         return dval
+
+
+def zero_(t: torch.Tensor) -> torch.Tensor:
+    """t[:] = 0 on the device (cudaMemsetAsync on the current stream)."""
+    dev = _require_cuda(t)
+    rc = _lib.load().sblas_zero(_ptr(t), t.numel() * t.element_size(), _stream_ptr(dev))
+    _lib.check(rc)
+    return t
 
 
 def csr_transpose(m: int, n: int, rowptr: torch.Tensor,

@@ -54,12 +54,13 @@ def batch_s(matrices, xs, k: int, candidates=(4, 8, 16, 32), reps: int = 5):
 
 
 def spmm_s(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, n: int, k: int,
-           candidates=(4, 8, 16, 32), reps: int = 5):
+           candidates=(4, 8, 16, 32), reps: int = 5, row_ids: torch.Tensor | None = None,
+           m_out: int | None = None, val_perm: torch.Tensor | None = None):
     """Best s for ops.SpmmPlan(rowptr, col, val, n, k); returns (s, {s: ms}).
     Times Y = A X on a scratch X of ones (the schedule does not depend on
     the values of X)."""
-    m = rowptr.numel() - 1
-    key = ("spmm", m, n, col.numel(), ops._val_kind(val), k)
+    m = rowptr.numel() - 1 if m_out is None else int(m_out)
+    key = ("spmm", rowptr.numel() - 1, m, n, col.numel(), ops._val_kind(val), k)
     if key in _CACHE:
         return _CACHE[key]
     dev = rowptr.device
@@ -67,7 +68,8 @@ def spmm_s(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, n:
     y = torch.empty((m, k) if k > 1 else (m,), dtype=torch.float64, device=dev)
     times = {}
     for s in candidates:
-        plan = ops.SpmmPlan(rowptr, col, val, n=n, k=k, s=s)
+        plan = ops.SpmmPlan(rowptr, col, val, n=n, k=k, s=s, row_ids=row_ids, m_out=m_out,
+                            val_perm=val_perm)
         times[s] = _time_ms(lambda: plan(x, y), reps)
         plan.close()
     best = min(times, key=times.get)

@@ -175,6 +175,15 @@ typedef struct sblas_batch_matrix {
     int ldy;
     double alpha;
     double beta;
+    /* NULL, or m distinct row indices of Y (ascending): stored row r of the
+     * matrix is row row_ids[r] of Y, and rows of Y not listed are left
+     * untouched.  Lets a matrix with many empty rows be stored without them
+     * (its row pointer then has one entry per listed row, plus one). */
+    const int *row_ids;
+    /* NULL, or nnz indices into val: stored entry p has value
+     * val[val_perm[p]] (a transposed pattern reading the values of the
+     * untransposed matrix, see sblas_csr_transpose). */
+    const int *val_perm;
 } sblas_batch_matrix;
 
 typedef struct sblas_batch_plan sblas_batch_plan;
@@ -218,6 +227,8 @@ SBLAS_API int sblas_csr_transpose(int m, int n, long long nnz, const int *rowptr
 /* dst[p] = src[perm[p]] for nnz values of the given kind (FP64 or FP32). */
 SBLAS_API int sblas_gather_values(long long nnz, int val_kind, const void *src, const int *perm,
                                   void *dst, void *stream);
+/* Zero `bytes` bytes of device memory at p, stream-ordered (cudaMemsetAsync). */
+SBLAS_API int sblas_zero(void *p, size_t bytes, void *stream);
 
 #ifdef __cplusplus
 }

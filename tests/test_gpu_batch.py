@@ -166,3 +166,31 @@ def test_batch_rejects_misaligned_x(sblas_lib, cuda):
     y = torch.zeros((1, 2), dtype=torch.float64, device=cuda)
     with pytest.raises(_lib.SblasError):
         ops.BatchPlan([(rp, col, val)], [x], [y], 2)
+
+
+@pytest.mark.parametrize("k", [1, 8])
+def test_row_ids_write_listed_rows_only(sblas_lib, cuda, k):
+    """A matrix stored without its empty rows (row_ids lists the rows of Y
+    that stored rows write): listed rows equal the full product, unlisted
+    rows keep their contents."""
+    from hpda_sblas_pnnl_gb300 import ops
+    g = load_golden("empty_rows")
+    rp = g["rowptr"].astype(np.int64)
+    m, n = int(g["m"]), int(g["n"])
+    keep = np.nonzero(rp[1:] > rp[:-1])[0]
+    rp_c = np.concatenate([rp[keep], rp[-1:]]).astype(np.int32)
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(device=cuda, dtype=dt)
+    x = torch.rand((n, k) if k > 1 else (n,), dtype=torch.float64, device=cuda)
+    y0 = torch.full((m, k) if k > 1 else (m,), 7.0, dtype=torch.float64, device=cuda)
+    y = y0.clone()
+    mat = (t(rp_c, torch.int32), t(g["col"], torch.int32), t(g["val"], torch.float64),
+           t(keep, torch.int32))
+    plan = ops.BatchPlan([mat], [x], [y], k, alpha=2.0, beta=0.5)
+    plan()
+    torch.cuda.synchronize()
+    full = O.csr_spmm(m, n, g["rowptr"].astype(np.int32), g["col"].astype(np.int32),
+                      g["val"].astype(np.float64), x.cpu().numpy(), y0.cpu().numpy(), 2.0, 0.5)
+    yy = y.cpu().numpy()
+    assert rel_l2(yy[keep], full[keep]) <= RTOL_L2
+    rest = np.setdiff1d(np.arange(m), keep)
+    assert (yy[rest] == 7.0).all()
