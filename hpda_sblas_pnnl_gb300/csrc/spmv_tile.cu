@@ -8,25 +8,29 @@
 // here CTA tiles of TILE = THREADS * SIGMA nonzeros and, inside a tile,
 // per-thread chunks of SIGMA consecutive nonzeros.
 //
-// Design for GB300 (measured: the FP64 pipe retires ~1.57e10 warp
-// instructions/s whatever the number of active lanes, i.e. ~0.5 T DFMA/s,
-// while HBM delivers ~7 TB/s = ~0.55 T nonzeros/s at 12-13 B/nonzero):
-//  * every thread runs exactly SIGMA fused multiply-adds with all 32 lanes
+// Design for GB300 (measured: the FP64 pipe retires ~1.65e10 warp
+// instructions/s whatever the number of active lanes, i.e. ~0.53 T DFMA/s;
+// random 32-byte L2->SM gathers run at ~2.8e11/s, one per nonzero):
+//  * warp-specialised persistent CTA: 4 compute warps (one chunk of SIGMA
+//    nonzeros per lane), a producer warp staging tiles into a STAGES-deep
+//    shared-memory ring with 1-D bulk copies (cp.async.bulk, L2 evict-first),
+//    and an epilogue warp merging the chunk carries one tile behind;
+//    mbarrier hand-offs, every wait bounded, no CTA-wide barrier in the loop;
+//  * every lane runs exactly SIGMA fused multiply-adds with all 32 lanes
 //    active; a row ending inside the chunk only costs integer work and a
 //    shared-memory store (the running sum restarts with a select);
-//  * the per-thread partial of the row crossing a chunk boundary ("tail") is
-//    combined at CTA level: one warp reduces runs of equal rows lane-
-//    sequentially (THREADS/32 adds per lane, work-efficient) and a 5-step
-//    segmented shuffle scan joins runs crossing lanes; the thread that holds
-//    the end of the row adds the result to its partial ("head") once;
+//  * the per-lane partial of the row crossing a chunk boundary ("tail") is
+//    combined by the epilogue warp: runs of equal rows reduced lane-
+//    sequentially (NCW adds per lane, work-efficient) and a 5-step segmented
+//    shuffle scan joining runs crossing lanes; the lane that holds the end of
+//    the row adds the result to its partial ("head") once;
 //  * rows are finished in a coalesced epilogue (alpha/beta applied once per
 //    row, nothing at all when alpha = 1 and beta = 0);
 //  * the row crossing a tile boundary is finished by a tiny fix-up kernel
 //    that adds the FP64 carries in a fixed order (no atomics: results are
 //    bit-reproducible run to run);
-//  * val/col tiles are streamed with 1-D bulk TMA (cp.async.bulk) into a
-//    two-stage shared-memory ring (L2 evict-first), x is gathered with an L2
-//    evict-last hint, grids are persistent (a multiple of the SM count).
+//  * x is gathered with an L2 evict-last hint; grids are persistent
+//    (occupancy x SM count), tiles round-robin over CTAs.
 #include <cstdio>
 #include <climits>
 
@@ -65,7 +69,7 @@ struct ValTraits<VAL_PATTERN> {
 
 constexpr int NCW = 4;                 // compute warps per CTA
 constexpr int TC = NCW * 32;           // compute threads per CTA (one chunk each)
-constexpr int CTA_THREADS = TC + 32;   // + one service warp
+constexpr int CTA_THREADS = TC + 64;   // + producer warp + epilogue warp
 
 template <int SIGMA, int VK>
 struct Layout {
@@ -144,7 +148,7 @@ struct Smem {
     __device__ uint64_t *cempty(int p) const { return bar() + 2 * STAGES + 2 + p; }
 };
 
-// Stages tile `tile` into stage `s` (the service warp, all lanes): owned-row
+// Stages tile `tile` into stage `s` (the producer warp, all lanes): owned-row
 // range (R0, R1), val and col by bulk copy, the row-pointer slice
 // rowptr[R0 .. R1+1] by bulk copy of its 16-byte-aligned superset; ragged
 // ends (and everything when a pointer is not 16-byte aligned) by plain loads
@@ -222,7 +226,7 @@ __device__ __forceinline__ double widen_f32(float v)
 // nonzeros per lane.  Row sums completed inside the chunk go to the carry
 // buffer of the tile's parity; the chunk's head (first segment of a row
 // begun earlier) and tail (partial of the row crossing the chunk end) are
-// published for the service warp.  No CTA-wide barrier.
+// published for the epilogue warp.  No CTA-wide barrier.
 template <int SIGMA, int VK, int AB>
 __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
                                              int cw, int lane, uint64_t pol_x)
@@ -379,21 +383,13 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
     }
 }
 
-// Service warp: stages tiles (producer) and, one tile behind the compute
-// warps, merges the chunk carries of each tile and writes its rows.
-//   carry pass: runs of equal rows among the TC tails are reduced lane-
-//   sequentially (NCW tails per lane, work-efficient), a 5-step segmented
-//   shuffle scan joins runs crossing lanes; each run total goes to the head
-//   of the chunk where the row ends, to a complete row, or to the tile carry;
-//   head pass: head + carry-in, one converged add per chunk;
-//   epilogue: alpha/beta once per row, coalesced stores of y.
-template <int SIGMA, int VK, int AB>
-__device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
-                                             int lane, uint64_t pol_stream)
+// Producer warp: stages the CTA's tiles into the STAGES-deep ring, each as
+// soon as the compute warps release its stage; the tile's partition entries
+// are loaded before that wait, so their latency hides behind it.
+template <int SIGMA, int VK>
+__device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+                                              int lane, uint64_t pol_stream)
 {
-    using L = Layout<SIGMA, VK>;
-    constexpr int PER = NCW;  // tails reduced per lane
-    const double alpha = a.alpha, beta = a.beta;
     int issued[STAGES];
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) issued[s] = 0;
@@ -405,41 +401,52 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
             ++issued[s];
         }
     }
-    double *cin = sm.cin();
-    // partition entries of the tile staged at iteration i (tile + STAGES*G),
-    // loaded one iteration ahead so their DRAM latency stays hidden
-    int nR0 = 0, nR1 = 0;
-    {
-        const int nt0 = blockIdx.x + STAGES * (int)gridDim.x;
-        if (nt0 < a.ntiles) {
-            nR0 = __ldg(a.row_part + nt0);
-            nR1 = __ldg(a.row_part + nt0 + 1);
-        }
-    }
-    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+    for (int i = 0, nt = blockIdx.x + STAGES * (int)gridDim.x; nt < a.ntiles;
+         ++i, nt += gridDim.x) {
         const int s = i % STAGES;
-        const int p = i & 1;
-        const int nt = tile + STAGES * (int)gridDim.x;
-        const int nt2 = nt + (int)gridDim.x;
-        int fR0 = 0, fR1 = 0;
-        if (nt2 < a.ntiles) {
-            fR0 = __ldg(a.row_part + nt2);
-            fR1 = __ldg(a.row_part + nt2 + 1);
-        }
-        bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1), WAIT_LIMIT_NS);
-        if (ok && nt < a.ntiles)
-            ok = ptx::mbar_wait_bounded(sm.empty(s), (uint32_t)((i / STAGES) & 1), WAIT_LIMIT_NS);
+        const int R0 = __ldg(a.row_part + nt);
+        const int R1 = __ldg(a.row_part + nt + 1);
+        const bool ok = ptx::mbar_wait_bounded(sm.empty(s), (uint32_t)((i / STAGES) & 1),
+                                               WAIT_LIMIT_NS);
         if (!__all_sync(0xffffffffu, ok)) {
             if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
             break;
         }
-        if (nt < a.ntiles) {
-            ptx::fence_proxy_async_smem();
-            produce_tile<SIGMA, VK>(a, sm, nt, s, nR0, nR1, lane, pol_stream);
-            ++issued[s];
+        ptx::fence_proxy_async_smem();
+        produce_tile<SIGMA, VK>(a, sm, nt, s, R0, R1, lane, pol_stream);
+        ++issued[s];
+    }
+    // the CTA may exit only when no copy into its shared memory is in flight
+    if (lane == 0) {
+        for (int s = 0; s < STAGES; ++s)
+            if (issued[s] > 0)
+                ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((issued[s] - 1) & 1), WAIT_LIMIT_NS);
+    }
+}
+
+// Epilogue warp: one tile behind the compute warps, merges the chunk
+// carries of each tile and writes its rows.
+//   carry pass: runs of equal rows among the TC tails are reduced lane-
+//   sequentially (NCW tails per lane, work-efficient), a 5-step segmented
+//   shuffle scan joins runs crossing lanes; each run total goes to the head
+//   of the chunk where the row ends, to a complete row, or to the tile carry;
+//   head pass: head + carry-in, one converged add per chunk;
+//   epilogue: alpha/beta once per row, coalesced stores of y.
+template <int SIGMA, int VK, int AB>
+__device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+                                              int lane)
+{
+    constexpr int PER = NCW;  // tails reduced per lane
+    const double alpha = a.alpha, beta = a.beta;
+    double *cin = sm.cin();
+    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+        const int p = i & 1;
+        const bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1),
+                                               WAIT_LIMIT_NS);
+        if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            break;
         }
-        nR0 = fR0;
-        nR1 = fR1;
         const int *cm = sm.cmeta(p);
         const int R0 = cm[0], R1 = cm[1];
         const bool fits = cm[2] != 0;
@@ -543,12 +550,6 @@ __device__ __forceinline__ void service_warp(const TileArgs &a, const Smem<SIGMA
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(sm.cempty(p));
     }
-    // drain: copies issued into a stage and never consumed (early exit only)
-    if (lane == 0) {
-        for (int s = 0; s < STAGES; ++s)
-            if (issued[s] > 0)
-                ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((issued[s] - 1) & 1), WAIT_LIMIT_NS);
-    }
 }
 
 template <int SIGMA, int VK, int AB>
@@ -575,7 +576,9 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
     for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
     __syncthreads();
     if (warp == NCW)
-        service_warp<SIGMA, VK, AB>(a, sm, lane, ptx::policy_evict_first());
+        producer_warp<SIGMA, VK>(a, sm, lane, ptx::policy_evict_first());
+    else if (warp == NCW + 1)
+        epilogue_warp<SIGMA, VK, AB>(a, sm, lane);
     else
         compute_warp<SIGMA, VK, AB>(a, sm, warp, lane, ptx::policy_evict_last());
 }
