@@ -77,12 +77,6 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_dcsrmv_analysed": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_double, _vp,
                                         C.c_int, _vp, _vp, _vp, C.c_double, _vp, C.c_int, _vp,
                                         C.c_size_t, _vp]),
-    "sblas_tile_hot_workspace_bytes": (C.c_size_t, [C.c_longlong, C.c_int]),
-    "sblas_csr_analyse_hot": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, _vp, _vp, C.c_int,
-                                        _vp, C.c_size_t, _vp]),
-    "sblas_dcsrmv_analysed_hot": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_double,
-                                            _vp, C.c_int, _vp, _vp, C.c_double, _vp, C.c_int, _vp,
-                                            C.c_size_t, _vp]),
     "sblas_noalloc_scratch_bytes": (C.c_size_t, []),
     "sblas_dcsrmv_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, _vp, _vp,
                                        C.c_double, _vp, _vp]),

@@ -226,82 +226,6 @@ int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, double alpha,
                             static_cast<cudaStream_t>(stream), true);
 }
 
-// Workspace of a hot-column plan: the tile workspace, then the remapped
-// column array, the hot-column table and its size.
-namespace {
-size_t hot_off_col(long long nnz, int sigma) { return tile_workspace_bytes(nnz, sigma); }
-size_t hot_off_tab(long long nnz, int sigma)
-{
-    return hot_off_col(nnz, sigma) + ((sizeof(int) * (size_t)(nnz > 0 ? nnz : 1) + 255) & ~size_t(255));
-}
-size_t hot_off_cnt(long long nnz, int sigma) { return hot_off_tab(nnz, sigma) + sizeof(int) * kHotMax; }
-}  // namespace
-
-size_t sblas_tile_hot_workspace_bytes(long long nnz, int sigma)
-{
-    if (sigma <= 0) sigma = default_sigma_for(0, nnz);
-    return hot_off_cnt(nnz, sigma) + 256;
-}
-
-int sblas_csr_analyse_hot(int kernel, int m, int n, long long nnz, const int *rowptr,
-                          const int *col, int sigma, void *work, size_t work_bytes, void *stream)
-{
-    clear_error();
-    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL || kernel < 2 || kernel > 3 ||
-        work == nullptr || (nnz > 0 && (rowptr == nullptr || col == nullptr))) {
-        set_error(SBLAS_ERR_ARG, "sblas_csr_analyse_hot: bad arguments");
-        return SBLAS_ERR_ARG;
-    }
-    if (sigma <= 0)
-        sigma = (kernel == SBLAS_KERNEL_CSR5) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
-    if (work_bytes < sblas_tile_hot_workspace_bytes(nnz, sigma) ||
-        (reinterpret_cast<uintptr_t>(work) & 255) != 0) {
-        set_error(SBLAS_ERR_ARG, "workspace needs %zu bytes at 256-byte alignment",
-                  sblas_tile_hot_workspace_bytes(nnz, sigma));
-        return SBLAS_ERR_ARG;
-    }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    unsigned char *w = static_cast<unsigned char *>(work);
-    const int rc = launch_tile_analyse(m, nnz, rowptr, sigma, work, st);
-    if (rc != SBLAS_OK) return rc;
-    return launch_hot_analyse(n, nnz, col, reinterpret_cast<int *>(w + hot_off_col(nnz, sigma)),
-                              reinterpret_cast<int *>(w + hot_off_tab(nnz, sigma)),
-                              reinterpret_cast<int *>(w + hot_off_cnt(nnz, sigma)), st);
-}
-
-int sblas_dcsrmv_analysed_hot(int kernel, int m, int n, long long nnz, double alpha,
-                              const void *val, int val_kind, const int *rowptr, const double *x,
-                              double beta, double *y, int sigma, void *work, size_t work_bytes,
-                              void *stream)
-{
-    clear_error();
-    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL || kernel < 2 || kernel > 3 ||
-        work == nullptr || val_kind < SBLAS_VAL_F64 || val_kind > SBLAS_VAL_PATTERN) {
-        set_error(SBLAS_ERR_ARG, "sblas_dcsrmv_analysed_hot: bad arguments");
-        return SBLAS_ERR_ARG;
-    }
-    if (m == 0) return SBLAS_OK;
-    if (y == nullptr || (nnz > 0 && (rowptr == nullptr || x == nullptr ||
-                                     (val_kind != SBLAS_VAL_PATTERN && val == nullptr)))) {
-        set_error(SBLAS_ERR_ARG, "null device pointer");
-        return SBLAS_ERR_ARG;
-    }
-    if (sigma <= 0)
-        sigma = (kernel == SBLAS_KERNEL_CSR5) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
-    if (work_bytes < sblas_tile_hot_workspace_bytes(nnz, sigma) ||
-        (reinterpret_cast<uintptr_t>(work) & 255) != 0) {
-        set_error(SBLAS_ERR_ARG, "workspace needs %zu bytes at 256-byte alignment",
-                  sblas_tile_hot_workspace_bytes(nnz, sigma));
-        return SBLAS_ERR_ARG;
-    }
-    unsigned char *w = static_cast<unsigned char *>(work);
-    return launch_tile_spmv(m, n, nnz, alpha, val, val_kind, rowptr,
-                            reinterpret_cast<const int *>(w + hot_off_col(nnz, sigma)), x, beta, y,
-                            sigma, work, static_cast<cudaStream_t>(stream), true,
-                            reinterpret_cast<const int *>(w + hot_off_tab(nnz, sigma)),
-                            reinterpret_cast<const int *>(w + hot_off_cnt(nnz, sigma)));
-}
-
 int sblas_dcoomv(int m, int n, long long nnz, double alpha, const double *val,
                  const int *coo_row, const int *coo_col, const double *x, double beta,
                  double *y, int *rowptr_work, int sigma, void *work, size_t work_bytes,

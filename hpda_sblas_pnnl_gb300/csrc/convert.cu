@@ -292,84 +292,3 @@ int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
 }
 
 }  // namespace sblas
-
-// ---- hot columns of a CSR matrix (analysis for the tile kernel) ----------
-namespace sblas {
-namespace {
-
-__global__ void col_histogram_kernel(long long nnz, const int *__restrict__ col, int *counts)
-{
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
-         p += (long long)gridDim.x * blockDim.x)
-        atomicAdd(counts + __ldg(col + p), 1);
-}
-
-// keys sorted by decreasing use: the hot slots are the leading columns used
-// at least twice, at most kHotMax of them
-__global__ void hot_select_kernel(int n, const int *__restrict__ keys_sorted,
-                                  const int *__restrict__ cols_sorted, int *hot_cols, int *nhot,
-                                  int *rank)
-{
-    const int lim = n < kHotMax ? n : kHotMax;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += gridDim.x * blockDim.x) {
-        const bool hot = keys_sorted[i] >= 2;
-        const bool next_cold = (i + 1 >= lim) || keys_sorted[i + 1] < 2;
-        if (hot) {
-            hot_cols[i] = cols_sorted[i];
-            rank[cols_sorted[i]] = i;
-        }
-        if (i == 0 && !hot) *nhot = 0;
-        if (hot && next_cold) *nhot = i + 1;
-    }
-}
-
-__global__ void hot_remap_kernel(long long nnz, const int *__restrict__ col,
-                                 const int *__restrict__ rank, int *__restrict__ col_out)
-{
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int c = __ldg(col + p);
-        const int r = __ldg(rank + c);
-        col_out[p] = r >= 0 ? ~r : c;
-    }
-}
-
-}  // namespace
-
-int launch_hot_analyse(int n, long long nnz, const int *col, int *col_out, int *hot_cols,
-                       int *nhot, cudaStream_t stream)
-{
-    if (n <= 0 || nnz <= 0) {
-        SBLAS_CUDA_TRY(cudaMemsetAsync(nhot, 0, sizeof(int), stream));
-        return SBLAS_OK;
-    }
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairsDescending<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                                        (int *)nullptr, (const int *)nullptr,
-                                                        (int *)nullptr, n);
-    const size_t vec = al256(sizeof(int) * (size_t)n);
-    unsigned char *w = static_cast<unsigned char *>(device_scratch(12, al256(cub_bytes) + 5 * vec));
-    if (!w) {
-        set_error(SBLAS_ERR_ALLOC, "cannot allocate the hot-column analysis scratch");
-        return SBLAS_ERR_ALLOC;
-    }
-    int *counts = reinterpret_cast<int *>(w + al256(cub_bytes));
-    int *keys_sorted = reinterpret_cast<int *>(w + al256(cub_bytes) + vec);
-    int *iota = reinterpret_cast<int *>(w + al256(cub_bytes) + 2 * vec);
-    int *cols_sorted = reinterpret_cast<int *>(w + al256(cub_bytes) + 3 * vec);
-    int *rank = reinterpret_cast<int *>(w + al256(cub_bytes) + 4 * vec);
-    SBLAS_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)n, stream));
-    SBLAS_CUDA_TRY(cudaMemsetAsync(rank, 0xFF, sizeof(int) * (size_t)n, stream));
-    col_histogram_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, col, counts);
-    iota_kernel<<<grid_for(n, 256), 256, 0, stream>>>(n, iota);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairsDescending<int, int>(
-        w, cub_bytes, counts, keys_sorted, iota, cols_sorted, n, 0, 32, stream)));
-    hot_select_kernel<<<(kHotMax + 255) / 256, 256, 0, stream>>>(n, keys_sorted, cols_sorted,
-                                                                  hot_cols, nhot, rank);
-    hot_remap_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, col, rank, col_out);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    return SBLAS_OK;
-}
-
-}  // namespace sblas

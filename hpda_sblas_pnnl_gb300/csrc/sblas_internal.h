@@ -52,21 +52,10 @@ enum ValueKind { VAL_F64 = 0, VAL_F32 = 1, VAL_PATTERN = 2 };
 // `work` must hold tile_workspace_bytes(nnz, sigma) bytes, 256-byte aligned.
 // analysed = true: the partition of `work` was computed by
 // launch_tile_analyse for this row pointer and sigma (skipped here).
-// hot_cols / nhot (device): the hot-column table of an analysed plan
-// (launch_hot_analyse); col then holds the remapped columns.
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
                      int val_kind, const int *rowptr, const int *col, const double *x,
                      double beta, double *y, int sigma, void *work, cudaStream_t stream,
-                     bool analysed = false, const int *hot_cols = nullptr,
-                     const int *nhot = nullptr);
-// Hot columns of a CSR column array for the tile kernel: the (up to) 4096
-// columns used most often (used at least twice; ties by column index),
-// hot_cols[k] = column of slot k, *nhot = slots used, col_out[p] = ~slot for
-// entries in a hot column, else col[p].  Allocates its temporaries in the
-// library's scratch (setup work).
-constexpr int kHotMax = 4096;
-int launch_hot_analyse(int n, long long nnz, const int *col, int *col_out, int *hot_cols,
-                       int *nhot, cudaStream_t stream);
+                     bool analysed = false);
 int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void *work,
                         cudaStream_t stream);
 

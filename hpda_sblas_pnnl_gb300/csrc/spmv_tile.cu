@@ -70,7 +70,6 @@ struct ValTraits<VAL_PATTERN> {
 constexpr int NCW = 4;                 // compute warps per CTA
 constexpr int TC = NCW * 32;           // compute threads per CTA (one chunk each)
 constexpr int CTA_THREADS = TC + 64;   // + producer warp + epilogue warp
-constexpr int HOT_MAX = kHotMax;       // x values of the most used columns kept per CTA
 
 template <int SIGMA, int VK>
 struct Layout {
@@ -114,10 +113,6 @@ struct TileArgs {
     int *status;          // [1]
     int use_tma;          // val and col 16-byte aligned: bulk copies
     int rp_tma;           // rowptr 16-byte aligned: bulk copies of its tile slices
-    // hot columns (analysed plans): col[p] < 0 names hot column ~col[p], whose
-    // x value every CTA keeps in shared memory; nullptr: no hot columns
-    const int *hot_cols;  // [HOT_MAX] original column of each hot slot
-    const int *nhot;      // [1] hot slots in use
 };
 
 // y epilogue for one finished row value v.
@@ -147,8 +142,6 @@ struct Smem {
     __device__ int *headk(int p) const { return reinterpret_cast<int *>(base + L::HEADK) + p * TC; }
     __device__ int *cmeta(int p) const { return reinterpret_cast<int *>(base + L::CMETA) + 4 * p; }
     __device__ uint64_t *bar() const { return reinterpret_cast<uint64_t *>(base + L::BAR); }
-    // hot-column x values, after the layout (present when the launch asks for them)
-    __device__ double *hotx() const { return reinterpret_cast<double *>(base + align16(L::TOTAL)); }
     __device__ uint64_t *full(int s) const { return bar() + s; }
     __device__ uint64_t *empty(int s) const { return bar() + STAGES + s; }
     __device__ uint64_t *cfull(int p) const { return bar() + 2 * STAGES + p; }
@@ -279,15 +272,7 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
             // issue every gather of the chunk first (one L2 round trip per
             // chunk instead of one per nonzero); the row search below runs
             // while they are in flight
-            if (a.hot_cols) {
-                // a hot column's x comes from shared memory, the others from L2
-                const uint32_t hbase = ptx::smem_addr(sm.hotx());
-#pragma unroll
-                for (int j = 0; j < SIGMA; ++j) {
-                    const int c = cst[c0 + (j < cnt ? j : 0)];
-                    xv[j] = ptx::ldg_x_or_shared(a.x + c, hbase + 8u * (uint32_t)(~c), c >= 0, pol_x);
-                }
-            } else if (cnt == SIGMA) {
+            if (cnt == SIGMA) {
 #pragma unroll
                 for (int j = 0; j < SIGMA; ++j)
                     xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + j], pol_x);
@@ -589,11 +574,6 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
     for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
-    if (a.hot_cols) {
-        const int nh = min(*a.nhot, HOT_MAX);
-        double *hx = sm.hotx();
-        for (int i = tid; i < nh; i += CTA_THREADS) hx[i] = __ldg(a.x + __ldg(a.hot_cols + i));
-    }
     __syncthreads();
     if (warp == NCW)
         producer_warp<SIGMA, VK>(a, sm, lane, ptx::policy_evict_first());
@@ -665,32 +645,26 @@ int launch_shape(const TileArgs &a, cudaStream_t stream)
 {
     using L = Layout<SIGMA, VK>;
     auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
-    // two shared-memory sizes: without and with the hot-column x values
-    constexpr size_t smem_plain = L::TOTAL;
-    constexpr size_t smem_hot = align16(L::TOTAL) + size_t(HOT_MAX) * 8;
     static int configured_dev = -1;
-    static int blocks_per_sm[2] = {0, 0};
+    static int blocks_per_sm = 0;
     int dev = 0;
     SBLAS_CUDA_TRY(cudaGetDevice(&dev));
     if (configured_dev != dev) {
         SBLAS_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem_hot));
-        for (int h = 0; h < 2; ++h) {
-            int bps = 0;
-            SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &bps, kfn, CTA_THREADS, h ? smem_hot : smem_plain));
-            if (bps < 1) {
-                set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
-                          SIGMA);
-                return SBLAS_ERR_UNSUPPORTED;
-            }
-            blocks_per_sm[h] = bps;
+                                            (int)L::TOTAL));
+        int bps = 0;
+        SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA_THREADS,
+                                                                     L::TOTAL));
+        if (bps < 1) {
+            set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
+                      SIGMA);
+            return SBLAS_ERR_UNSUPPORTED;
         }
+        blocks_per_sm = bps;
         configured_dev = dev;
     }
-    const int h = a.hot_cols ? 1 : 0;
-    const int grid = min(a.ntiles, blocks_per_sm[h] * device_num_sms());
-    kfn<<<grid, CTA_THREADS, h ? smem_hot : smem_plain, stream>>>(a);
+    const int grid = min(a.ntiles, blocks_per_sm * device_num_sms());
+    kfn<<<grid, CTA_THREADS, L::TOTAL, stream>>>(a);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }
@@ -797,8 +771,7 @@ int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void
 
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val, int val_kind,
                      const int *rowptr, const int *col, const double *x, double beta, double *y,
-                     int sigma, void *work, cudaStream_t stream, bool analysed,
-                     const int *hot_cols, const int *nhot)
+                     int sigma, void *work, cudaStream_t stream, bool analysed)
 {
     if (m <= 0) return SBLAS_OK;
     if (nnz <= 0) return launch_scale_y(m, beta, y, stream);
@@ -841,8 +814,6 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     const uintptr_t vb = reinterpret_cast<uintptr_t>(val), cb = reinterpret_cast<uintptr_t>(col);
     a.use_tma = ((val_kind == VAL_PATTERN || (vb & 15) == 0) && (cb & 15) == 0) ? 1 : 0;
     a.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
-    a.hot_cols = hot_cols;
-    a.nhot = nhot;
     int rc = SBLAS_OK;
     switch (sigma) {
     case 11: rc = launch_vk<11>(val_kind, a, stream); break;

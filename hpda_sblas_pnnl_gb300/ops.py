@@ -142,14 +142,11 @@ class CsrPlan:
     The tile partition of the row pointer is computed at construction
     (sblas_csr_analyse) into a workspace owned by the plan; each call runs
     only the tile kernel and the carry fix-up (sblas_dcsrmv_analysed), does
-    not allocate and can be captured in a CUDA graph.  hot=True also finds
-    the most used columns (sblas_csr_analyse_hot): their x values are served
-    from shared memory (same results; n is needed, taken from col if None).
+    not allocate and can be captured in a CUDA graph.
     """
 
     def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
-                 n: int | None = None, kernel: int = KERNEL_MERGEPATH, sigma: int = 0,
-                 hot: bool = False):
+                 n: int | None = None, kernel: int = KERNEL_MERGEPATH, sigma: int = 0):
         dev = _require_cuda(rowptr, col, val)
         if kernel not in (KERNEL_MERGEPATH, KERNEL_CSR5):
             raise ValueError("plans use the tile kernels (2 or 3)")
@@ -171,39 +168,18 @@ class CsrPlan:
             self.vk = VAL_F32
         else:
             raise TypeError("val must be float64, float32 or None")
-        self.hot = bool(hot)
-        if self.hot:
-            self.work_bytes = int(lib.sblas_tile_hot_workspace_bytes(self.nnz, self.sigma))
-        else:
-            self.work_bytes = int(lib.sblas_tile_workspace_bytes(self.nnz, self.sigma))
+        self.work_bytes = int(lib.sblas_tile_workspace_bytes(self.nnz, self.sigma))
         self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=dev)
         self.device = dev
         with torch.cuda.device(dev):
-            if self.hot:
-                nx = self.n if self.n is not None else int(col.max()) + 1 if self.nnz else 0
-                self.n = nx if self.n is None else self.n
-                rc = lib.sblas_csr_analyse_hot(kernel, self.m, self.n, self.nnz, _ptr(rowptr),
-                                               _ptr(col), self.sigma, _ptr(self.work),
-                                               self.work_bytes, _stream_ptr(dev))
-            else:
-                rc = lib.sblas_csr_analyse(kernel, self.m, self.nnz, _ptr(rowptr), self.sigma,
-                                           _ptr(self.work), self.work_bytes, _stream_ptr(dev))
+            rc = lib.sblas_csr_analyse(kernel, self.m, self.nnz, _ptr(rowptr), self.sigma,
+                                       _ptr(self.work), self.work_bytes, _stream_ptr(dev))
         _lib.check(rc)
 
     def __call__(self, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0,
                  beta: float = 0.0) -> torch.Tensor:
         n = self.n if self.n is not None else x.numel()
         lib = _lib.load()
-        if self.hot:
-            if x.numel() < n:
-                raise ValueError("x shorter than the matrix's column count")
-            rc = lib.sblas_dcsrmv_analysed_hot(self.kernel, self.m, n, self.nnz, float(alpha),
-                                               _ptr(self.val), self.vk, _ptr(self.rowptr),
-                                               _ptr(x), float(beta), _ptr(y), self.sigma,
-                                               _ptr(self.work), self.work_bytes,
-                                               _stream_ptr(self.device))
-            _lib.check(rc)
-            return y
         rc = lib.sblas_dcsrmv_analysed(self.kernel, self.m, n, self.nnz, float(alpha),
                                        _ptr(self.val), self.vk, _ptr(self.rowptr), _ptr(self.col),
                                        _ptr(x), float(beta), _ptr(y), self.sigma, _ptr(self.work),

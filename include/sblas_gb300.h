@@ -108,24 +108,6 @@ SBLAS_API int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, dou
                                     const int *col, const double *x, double beta, double *y,
                                     int sigma, void *work, size_t work_bytes, void *stream);
 
-/* Analysed plans with hot columns (kernel 2 or 3): sblas_csr_analyse_hot
- * does what sblas_csr_analyse does and also finds the (up to 4096) columns
- * used most often; their x values are then kept in every CTA's shared
- * memory, so the nonzeros in those columns gather x from shared memory
- * instead of L2 (on power-law graphs with skewed column use, ~40 % of all
- * nonzeros).  The plan stores a remapped copy of col in `work`; results are
- * bit-identical to sblas_dcsrmv_analysed.  The analysis allocates scratch
- * inside the library (setup work); the product allocates nothing.
- * work: sblas_tile_hot_workspace_bytes(nnz, sigma) bytes, 256-byte aligned. */
-SBLAS_API size_t sblas_tile_hot_workspace_bytes(long long nnz, int sigma);
-SBLAS_API int sblas_csr_analyse_hot(int kernel, int m, int n, long long nnz, const int *rowptr,
-                                    const int *col, int sigma, void *work, size_t work_bytes,
-                                    void *stream);
-SBLAS_API int sblas_dcsrmv_analysed_hot(int kernel, int m, int n, long long nnz, double alpha,
-                                        const void *val, int val_kind, const int *rowptr,
-                                        const double *x, double beta, double *y, int sigma,
-                                        void *work, size_t work_bytes, void *stream);
-
 /* Allocation-free FP64 CSR SpMV (the tile kernel, default tile shape) for
  * callers that cannot call cudaMalloc when they need it: code running inside
  * a device-memory pool or caching allocator, or services that reserve all

@@ -52,23 +52,6 @@ def test_powerlaw_csr_all_kernels(sblas_lib, cuda, powerlaw):
     assert abs(float(y.sum()) - float((cc * x).sum())) <= 1e-9 * float((cc * x).sum())
 
 
-def test_powerlaw_hot_column_plan(sblas_lib, cuda, powerlaw):
-    """Full-size power-law graph: the hot-column plan (most used columns' x
-    in shared memory) is bit-identical to the plain plan and matches the
-    oracle."""
-    from hpda_sblas_pnnl_gb300 import ops
-    a, x = powerlaw
-    ref = oracle_y(a, x)
-    for sg in (15, 19):
-        y1 = torch.zeros(a.m, dtype=torch.float64, device=cuda)
-        y2 = torch.full((a.m,), float("nan"), dtype=torch.float64, device=cuda)
-        ops.CsrPlan(a.rowptr, a.col, a.val, n=a.n, sigma=sg)(x, y1)
-        ops.CsrPlan(a.rowptr, a.col, a.val, n=a.n, sigma=sg, hot=True)(x, y2)
-        torch.cuda.synchronize()
-        np.testing.assert_array_equal(y2.cpu().numpy(), y1.cpu().numpy())
-        assert rel_l2(y2.cpu().numpy(), ref) <= 1e-12
-
-
 def test_powerlaw_alpha_beta_linearity(sblas_lib, cuda, powerlaw):
     """A(2x1 - 3x2) = 2Ax1 - 3Ax2 and y = a*A*x + b*y0 (size-independent)."""
     from hpda_sblas_pnnl_gb300 import ops

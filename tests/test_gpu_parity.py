@@ -303,23 +303,3 @@ def test_fp32_values_with_subnormals_and_huge_entries(sblas_lib, cuda):
     assert rel_l2(yy / scale, ref / scale) <= 1e-12
     small = np.abs(ref) < 1e30
     assert rel_l2(yy[small], ref[small]) <= 1e-12
-
-@pytest.mark.parametrize("name", ["zipf200_ab", "long_row", "empty_rows", "sparse_rows",
-                                  "diag3000", "g200", "one", "nnz0"])
-def test_hot_column_plans_are_bit_identical(sblas_lib, cuda, name):
-    """Plans that serve the most used columns' x from shared memory give the
-    same bits as the plain analysed plans (same summation order), for every
-    tile shape and value kind."""
-    from hpda_sblas_pnnl_gb300 import ops
-    g = load_golden(name)
-    n = int(g["n"])
-    a, b = float(g["alpha"]), float(g["beta"])
-    for s in sigmas():
-        for vk in ("f64", "f32", "pattern"):
-            rp, c, v, x, y = dev(g, cuda)
-            val = {"f64": v, "f32": v.float(), "pattern": None}[vk]
-            y2 = y.clone()
-            ops.CsrPlan(rp, c, val, n=n, sigma=s)(x, y, a, b)
-            ops.CsrPlan(rp, c, val, n=n, sigma=s, hot=True)(x, y2, a, b)
-            torch.cuda.synchronize()
-            np.testing.assert_array_equal(y2.cpu().numpy(), y.cpu().numpy())
