@@ -58,12 +58,16 @@ DeviceContext *device_context()
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return nullptr;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, cst = nullptr;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
     for (auto &e : c.ev)
         if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    for (auto &e : c.chunk_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
     c.num_sms = sms;
     c.stream = st;
+    c.copy_stream = cst;
     c.device = dev;
     return &c;
 }

@@ -129,6 +129,121 @@ bool check_kernel(const char *name, int kernel)
     return true;
 }
 
+// Row pointer of one chunk rebased to its first nonzero: out[i] = rp[i] - base.
+__global__ void rebase_rowptr_kernel(int count, const int *__restrict__ rp, int base, int *out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        out[i] = rp[i] - base;
+}
+
+constexpr long long kPipeMinNnz = 1LL << 22;   // smaller matrices: copy, then compute
+
+// Large CSR calls with host arrays: the matrix travels in kPipeChunks row
+// chunks of equal nonzero counts, each chunk's SpMV starting as soon as its
+// values and columns have arrived (copies on the context's copy stream, the
+// tile kernel on its compute stream, y of a chunk sent back right after its
+// kernel), so the kernels and the device-to-host copies hide behind the
+// host-to-device copies, which the host link bounds.  Each chunk's arrays
+// are placed at 256-byte aligned offsets so the tile kernel keeps its bulk
+// copies; its row pointer is rebased to the chunk's first nonzero.
+spmv_ret run_host_pipelined(const Call &c, DeviceContext *ctx)
+{
+    const int m = c.m, n = c.n;
+    const long long nnz = c.nnz;
+    const int K = kPipeChunks;
+    const bool need_y_in = (c.beta != 0.0) || c.additive;
+    cudaStream_t cs = ctx->copy_stream, ks = ctx->stream;
+    // chunk k: rows [r[k], r[k+1]), nonzeros [ptr[r[k]], ptr[r[k+1]])
+    int r[kPipeChunks + 1];
+    r[0] = 0;
+    r[K] = m;
+    for (int k = 1; k < K; ++k) {
+        const long long want = nnz * k / K;
+        int lo = r[k - 1], hi = m;   // first row with ptr[row] >= want
+        while (lo < hi) {
+            const int mid = lo + (hi - lo) / 2;
+            if (c.ptr[mid] >= want) hi = mid; else lo = mid + 1;
+        }
+        r[k] = lo;
+    }
+    const size_t pad = 256;
+    double *d_val = static_cast<double *>(device_scratch(1, sizeof(double) * (size_t)nnz + K * pad));
+    int *d_idx = static_cast<int *>(device_scratch(2, sizeof(int) * (size_t)nnz + K * pad));
+    int *d_ptr = static_cast<int *>(device_scratch(3, sizeof(int) * (size_t)(m + 1)));
+    double *d_x = static_cast<double *>(device_scratch(4, sizeof(double) * (size_t)n));
+    double *d_y = static_cast<double *>(device_scratch(5, sizeof(double) * (size_t)m));
+    int *d_rp = static_cast<int *>(device_scratch(8, sizeof(int) * (size_t)(m + 1 + K) + K * pad));
+    const int sigma = (c.kernel == 3) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
+    void *w = device_scratch(0, tile_workspace_bytes(nnz, sigma));
+    if (!d_val || !d_idx || !d_ptr || !d_x || !d_y || !d_rp || !w) {
+        set_error(SBLAS_ERR_ALLOC, "%s: device allocation failed", c.name);
+        return failed();
+    }
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1], e2 = ctx->ev[2], e3 = ctx->ev[3];
+    // ---- inputs every chunk needs: row pointer, x (and y when it is read)
+    DROPIN_CUDA(cudaEventRecord(e0, cs));
+    DROPIN_CUDA(cudaMemcpyAsync(d_ptr, c.ptr, sizeof(int) * (size_t)(m + 1), cudaMemcpyHostToDevice, cs));
+    DROPIN_CUDA(cudaMemcpyAsync(d_x, c.x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, cs));
+    if (need_y_in)
+        DROPIN_CUDA(cudaMemcpyAsync(d_y, c.y, sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, cs));
+    DROPIN_CUDA(cudaEventRecord(ctx->chunk_ev[0], cs));
+    // ---- the chunks' values and columns
+    size_t vo[kPipeChunks], io[kPipeChunks], ro[kPipeChunks];
+    size_t voff = 0, ioff = 0, roff = 0;
+    for (int k = 0; k < K; ++k) {
+        const long long lo = c.ptr[r[k]], hi = c.ptr[r[k + 1]];
+        vo[k] = voff;
+        io[k] = ioff;
+        ro[k] = roff;
+        if (hi > lo) {
+            DROPIN_CUDA(cudaMemcpyAsync(reinterpret_cast<unsigned char *>(d_val) + voff, c.val + lo,
+                                        sizeof(double) * (size_t)(hi - lo), cudaMemcpyHostToDevice, cs));
+            DROPIN_CUDA(cudaMemcpyAsync(reinterpret_cast<unsigned char *>(d_idx) + ioff, c.idx + lo,
+                                        sizeof(int) * (size_t)(hi - lo), cudaMemcpyHostToDevice, cs));
+        }
+        DROPIN_CUDA(cudaEventRecord(ctx->chunk_ev[1 + k], cs));
+        voff += up(sizeof(double) * (size_t)(hi - lo));
+        ioff += up(sizeof(int) * (size_t)(hi - lo));
+        roff += up(sizeof(int) * (size_t)(r[k + 1] - r[k] + 1));
+    }
+    DROPIN_CUDA(cudaEventRecord(e1, cs));
+    // ---- per chunk: rebase its row pointer, SpMV, send its rows of y back
+    DROPIN_CUDA(cudaStreamWaitEvent(ks, ctx->chunk_ev[0], 0));
+    DROPIN_CUDA(cudaEventRecord(e2, ks));
+    const double beta_eff = c.additive ? c.beta + 1.0 : c.beta;
+    for (int k = 0; k < K; ++k) {
+        const int rows = r[k + 1] - r[k];
+        if (rows == 0) continue;
+        const long long lo = c.ptr[r[k]], cnnz = c.ptr[r[k + 1]] - lo;
+        int *rp = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(d_rp) + ro[k]);
+        rebase_rowptr_kernel<<<(rows + 1 + 255) / 256 < 1024 ? (rows + 1 + 255) / 256 : 1024, 256, 0, ks>>>(
+            rows + 1, d_ptr + r[k], (int)lo, rp);
+        DROPIN_CUDA(cudaGetLastError());
+        DROPIN_CUDA(cudaStreamWaitEvent(ks, ctx->chunk_ev[1 + k], 0));
+        const double *val = reinterpret_cast<const double *>(reinterpret_cast<unsigned char *>(d_val) + vo[k]);
+        const int *col = reinterpret_cast<const int *>(reinterpret_cast<unsigned char *>(d_idx) + io[k]);
+        const int rc = (cnnz == 0)
+                           ? launch_scale_y(rows, beta_eff, d_y + r[k], ks)
+                           : launch_tile_spmv(rows, n, cnnz, c.alpha, val, SBLAS_VAL_F64, rp, col, d_x,
+                                              beta_eff, d_y + r[k], sigma, w, ks);
+        if (rc != SBLAS_OK) return failed();
+        DROPIN_CUDA(cudaMemcpyAsync(c.y + r[k], d_y + r[k], sizeof(double) * (size_t)rows,
+                                    cudaMemcpyDeviceToHost, ks));
+    }
+    DROPIN_CUDA(cudaEventRecord(e3, ks));
+    const double tm = wall();
+    DROPIN_CUDA(cudaEventSynchronize(e3));
+    spmv_ret ret = zero_ret();
+    float t_comm = 0.f, t_comp = 0.f;
+    DROPIN_CUDA(cudaEventElapsedTime(&t_comm, e0, e1));
+    DROPIN_CUDA(cudaEventElapsedTime(&t_comp, e2, e3));
+    ret.comm_time = t_comm * 1e-3;   // host-to-device copies (overlapping the kernels)
+    ret.comp_time = t_comp * 1e-3;   // kernels and the copies of y back, from the first chunk on
+    ret.merg_time = wall() - tm;
+    return ret;
+}
+
 // The engine behind every host entry point.
 spmv_ret run_host(Call c)
 {
@@ -140,6 +255,9 @@ spmv_ret run_host(Call c)
     }
     spmv_ret ret = zero_ret();
     if (c.m == 0) return ret;
+    if (c.fmt == Fmt::CSR && c.kernel != 1 && c.nnz >= kPipeMinNnz && c.n > 0 && c.row_lo == 0 &&
+        c.row_hi == c.m)
+        return run_host_pipelined(c, ctx);
     cudaStream_t st = ctx->stream;
     const int m = c.m, n = c.n;
     const long long nnz = c.nnz;

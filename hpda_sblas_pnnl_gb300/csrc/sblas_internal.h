@@ -95,11 +95,14 @@ int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
                   const double *in_d, double *out_d, cudaStream_t stream);
 
 // ---- per-device resources used by the host (drop-in) entry points --------
+constexpr int kPipeChunks = 4;   // chunks of the host-array entry points' copy/compute overlap
 struct DeviceContext {
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // host -> device copies overlapping the kernels
     cudaEvent_t ev[6] = {};
+    cudaEvent_t chunk_ev[kPipeChunks + 1] = {};  // copies done (inputs, then each chunk)
 };
 // Returns the context of the current device (created on first use).
 DeviceContext *device_context();

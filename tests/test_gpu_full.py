@@ -107,3 +107,28 @@ def test_banded_fp64_and_fp32_values(sblas_lib, cuda):
     ops.csrmv(a.rowptr, a.col, v32, x, y32)
     torch.cuda.synchronize()
     assert rel_l2(y32.cpu().numpy(), ref) <= 1e-6
+
+
+@pytest.mark.parametrize("kernel", [2, 3])
+def test_host_entry_point_overlapped_chunks(sblas_lib, cuda, kernel):
+    """Host-array calls large enough to be copied in row chunks overlapping
+    the kernels (6.4M nonzeros): same result as the oracle, with alpha,
+    beta and a y that is read, from pinned and from pageable host arrays."""
+    from hpda_sblas_pnnl_gb300 import api, synth
+    a, x = synth.powerlaw(m=400_000, mean_deg=17.5, seed=12, device=cuda, values="normal")
+    assert a.nnz > (1 << 22)
+    rp, c, v = a.numpy()
+    xx = x.cpu().numpy()
+    rng = np.random.default_rng(4)
+    y0 = rng.standard_normal(a.m)
+    ref = O.csr_spmv(a.m, a.n, rp, c, v, xx, y0, 1.5, -0.5, threads=THREADS)
+    for pinned in (True, False):
+        arr = (lambda t: torch.from_numpy(t).pin_memory().numpy()) if pinned else (lambda t: t.copy())
+        y = arr(y0.copy())
+        ret = api.spMV_mgpu_v1(a.m, a.n, a.nnz, 1.5, arr(v), arr(rp), arr(c), arr(xx), -0.5, y,
+                               kernel=kernel)
+        assert ret.comp_time >= 0 and ret.comm_time > 0
+        assert rel_l2(y, ref) <= 1e-12
+        y = arr(np.full(a.m, np.nan))
+        api.spMV_mgpu_baseline(a.m, a.n, a.nnz, 1.0, arr(v), arr(rp), arr(c), arr(xx), 0.0, y)
+        assert rel_l2(y, O.csr_spmv(a.m, a.n, rp, c, v, xx, np.zeros(a.m), threads=THREADS)) <= 1e-12
