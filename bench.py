@@ -68,6 +68,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(v: float, device) -> float:
+    """The maximum of v over the ranks of the initialised process group (v
+    itself without one): the job's time is its slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(v)
+    t = torch.tensor([float(v)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(bytes_per_rank: int, ms_step: float, world: int) -> float:
+    """Whole-job compulsory GB/s: every rank moves bytes_per_rank per step
+    (weak scaling, an independent instance per rank)."""
+    return world * bytes_per_rank / (ms_step * 1e-3) / 1e9
+
+
 def peaks():
     try:
         d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -130,7 +148,7 @@ def make_workload(device, seed, m=4_000_000):
     return a, x
 
 
-def cpu_time_spmv(a_np, x_np, m, n, reps, threads, use_ref):
+def cpu_time_spmv(a_np, x_np, m, n, reps, threads, use_ref, warmup=2):
     """Median seconds of the reference CPU loop on `threads` host threads."""
     import numpy as np
     from oracle import oracle as O
@@ -139,8 +157,8 @@ def cpu_time_spmv(a_np, x_np, m, n, reps, threads, use_ref):
     fn = (lambda: O.ref_csr_spmv(m, n, rp, col, val, x_np, y0, 1.0, 0.0, threads=threads)) \
         if use_ref else \
         (lambda: O.csr_spmv(m, n, rp, col, val, x_np, y0, 1.0, 0.0, threads=threads))
-    fn()
-    fn()
+    for _ in range(warmup):
+        fn()
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -160,23 +178,24 @@ def run_reference(args):
     from hpda_sblas_pnnl_gb300 import synth
     from oracle import oracle as O
     O.build() if not O.LIB.exists() else None
-    a, x = make_workload("cpu", args.seed)
+    a, x = make_workload("cpu", args.seed, args.m)
     m, n, nnz = a.m, a.n, a.nnz
     a_np = tuple(np.ascontiguousarray(t) for t in a.numpy())
     x_np = np.ascontiguousarray(x.numpy())
     threads = os.cpu_count() or 1
     use_ref = O.ref_available()
     bytes_step = synth.compulsory_bytes(m, n, nnz)
-    med, ts = cpu_time_spmv(a_np, x_np, m, n, max(args.steps, 1), threads, use_ref)
+    warm = max(args.warmup, 3)
+    med, ts = cpu_time_spmv(a_np, x_np, m, n, max(args.steps, 1), threads, use_ref, warm)
     # warmup and steps: every step is one full SpMV (a bounded sample: the
-    # whole matrix, ~0.1-1 s per step on the host)
+    # whole matrix, ~0.01-1 s per step on the host)
     total = sum(ts)
     value = bytes_step * len(ts) / total / 1e9
     kind = "reference" if use_ref else "port"
-    sample = f"full matrix ({nnz} nnz), {len(ts)} steps after 2 warm-up runs"
+    sample = f"full matrix ({nnz} nnz), {len(ts)} steps after {warm} warm-up runs"
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
-        "n_gpus": ws, "steps": len(ts), "warmup": 2, "ms_per_step": round(1e3 * total / len(ts), 3),
+        "n_gpus": ws, "steps": len(ts), "warmup": warm, "ms_per_step": round(1e3 * total / len(ts), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
         "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
@@ -257,13 +276,9 @@ def run_ours(args):
     if ws > 1:
         dist.barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dev)
     ms_step = ms / args.steps
-    value = ws * bytes_step / (ms_step * 1e-3) / 1e9
+    value = job_value(bytes_step, ms_step, ws)
     launches_per_step = 3
 
     # correctness of what was timed (oracle spot check on rank 0 is in the
