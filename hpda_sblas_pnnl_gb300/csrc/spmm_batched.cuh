@@ -89,10 +89,18 @@ struct Args {
     void *dval;            // FP64 or FP32 per the value kind
 };
 
+// Row stride (doubles) of the per-warp row and head buffers.  For K = 16 a
+// row is 128 bytes, so the rows lanes store at the same time would all start
+// in the same shared-memory bank: padded by two doubles.  Smaller K keep
+// their stride (the padding would cost them a CTA per SM, which measured
+// slower than the bank conflicts it removes).
+template <int K>
+constexpr int row_stride() { return K == 16 ? K + 2 : K; }
+
 template <int K, int S>
 struct Shape {
     static constexpr int UNIT = 32 * S;                        // nonzeros per unit
-    static constexpr int RCAP = (8 * S < 2048 / K) ? 8 * S : 2048 / K;  // rows in the buffer
+    static constexpr int RCAP = (8 * S < 1536 / K) ? 8 * S : 1536 / K;  // rows in the buffer
     static constexpr int RPN = RCAP + 2;                       // row-pointer slice entries
 };
 
@@ -122,8 +130,8 @@ struct WarpSmem {
     static constexpr size_t VAL = COL + size_t(SH::UNIT) * 4;
     static constexpr size_t RP = (VAL + size_t(SH::UNIT) * VT<VK>::B + 15) / 16 * 16;
     static constexpr size_t RBUF = (RP + size_t(SH::RPN) * 4 + 15) / 16 * 16;
-    static constexpr size_t HBUF = RBUF + size_t(SH::RCAP) * K * 8;
-    static constexpr size_t TOTAL = HBUF + size_t(32) * K * 8;
+    static constexpr size_t HBUF = RBUF + size_t(SH::RCAP) * row_stride<K>() * 8;
+    static constexpr size_t TOTAL = HBUF + size_t(32) * row_stride<K>() * 8;
 };
 
 template <int K, int S, int VK>
@@ -204,7 +212,8 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
     T *sval = reinterpret_cast<T *>(ws + WS::VAL);
     int *srp = reinterpret_cast<int *>(ws + WS::RP);
     double *rbuf = reinterpret_cast<double *>(ws + WS::RBUF);
-    double *hbuf = reinterpret_cast<double *>(ws + WS::HBUF) + lane * K;
+    constexpr int KP = row_stride<K>();
+    double *hbuf = reinterpret_cast<double *>(ws + WS::HBUF) + lane * KP;
     const uint64_t pol_x = ptx::policy_evict_last();
     const unsigned FULL = 0xffffffffu;
 
@@ -242,7 +251,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         }
         if (fits) {
             for (int i = lane; i <= rp_hi - RA; i += 32) srp[i] = __ldg(rowptr + RA + i);
-            for (int i = lane; i < nrows * K; i += 32) rbuf[i] = 0.0;
+            for (int i = lane; i < nrows * KP; i += 32) rbuf[i] = 0.0;
         }
         __syncwarp();
         auto rp = [&](int r) -> int { return fits ? srp[r - RA] : __ldg(rowptr + r); };
@@ -317,14 +326,14 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             // branch-free row emission: at a row start the running sums go to
             // the row buffer (or the head slot for a row begun before the
             // chunk) and restart
-            double *dst = sb ? hbuf : rbuf + (r0 - RA) * K;
-            double *nxp = rbuf + (r0 + 1 - RA) * K;
+            double *dst = sb ? hbuf : rbuf + (r0 - RA) * KP;
+            double *nxp = rbuf + (r0 + 1 - RA) * KP;
 #pragma unroll
             for (int j = 0; j < S; ++j) {
                 const bool bnd = (mask >> j) & 1u;
                 if (bnd) store_row<K>(dst, acc);
                 dst = bnd ? nxp : dst;
-                nxp = bnd ? nxp + K : nxp;
+                nxp = bnd ? nxp + KP : nxp;
 #pragma unroll
                 for (int c = 0; c < K; ++c) acc[c] = bnd ? 0.0 : acc[c];
                 if (j < cnt) step(j);
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                     has_head = true;
                     hrow = row;
                 } else if (fits) {
-                    store_row<K>(rbuf + (row - RA) * K, acc);
+                    store_row<K>(rbuf + (row - RA) * KP, acc);
                 } else {
                     double *yr = y + out_row(M, row) * ldy;
 #pragma unroll
@@ -416,7 +425,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                 a.head_row[u] = hrow;
                 store_row<K>(a.head_val + (long long)u * K, tot);
             } else if (fits) {
-                store_row<K>(rbuf + (hrow - RA) * K, tot);
+                store_row<K>(rbuf + (hrow - RA) * KP, tot);
             } else {
                 double *yr = y + out_row(M, hrow) * ldy;
 #pragma unroll
@@ -444,7 +453,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             for (int i = lane; i < ne; i += 32) {
                 const int rr = i / K, c = i - rr * K;
                 double *yp = y + out_row(M, E0 + rr) * ldy + c;
-                *yp = finish(rbuf[(E0 - RA + rr) * K + c], alpha, beta, yp);
+                *yp = finish(rbuf[(E0 - RA + rr) * KP + c], alpha, beta, yp);
             }
         } else {
             for (int r = E0 + lane; r < RB; r += 32)
