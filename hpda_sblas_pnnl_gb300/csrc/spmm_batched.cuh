@@ -127,8 +127,10 @@ template <int K, int S, int VK>
 struct WarpSmem {
     using SH = Shape<K, S>;
     static constexpr size_t COL = 0;
-    static constexpr size_t VAL = COL + size_t(SH::UNIT) * 4;
-    static constexpr size_t RP = (VAL + size_t(SH::UNIT) * VT<VK>::B + 15) / 16 * 16;
+    // staged col and val: lane l's S entries at l*(S+1) (an odd stride for the
+    // even S, so the lanes' strided reads hit different banks)
+    static constexpr size_t VAL = COL + size_t(SH::UNIT + 32) * 4;
+    static constexpr size_t RP = (VAL + size_t(SH::UNIT + 32) * VT<VK>::B + 15) / 16 * 16;
     static constexpr size_t RBUF = (RP + size_t(SH::RPN) * 4 + 15) / 16 * 16;
     static constexpr size_t HBUF = RBUF + size_t(SH::RCAP) * row_stride<K>() * 8;
     static constexpr size_t TOTAL = HBUF + size_t(32) * row_stride<K>() * 8;
@@ -241,13 +243,14 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
 
         // ---- stage the unit (coalesced), zero the row buffer ------------
         __syncwarp();
-        for (int i = lane; i < cntu; i += 32) scol[i] = __ldcs(col + U0 + i);
+        for (int i = lane; i < cntu; i += 32) scol[i + i / S] = __ldcs(col + U0 + i);
         if constexpr (VK != VAL_PATTERN) {
             const T *vp = static_cast<const T *>(val);
             if (M->val_perm)
-                for (int i = lane; i < cntu; i += 32) sval[i] = __ldg(vp + __ldcs(M->val_perm + U0 + i));
+                for (int i = lane; i < cntu; i += 32)
+                    sval[i + i / S] = __ldg(vp + __ldcs(M->val_perm + U0 + i));
             else
-                for (int i = lane; i < cntu; i += 32) sval[i] = __ldcs(vp + U0 + i);
+                for (int i = lane; i < cntu; i += 32) sval[i + i / S] = __ldcs(vp + U0 + i);
         }
         if (fits) {
             for (int i = lane; i <= rp_hi - RA; i += 32) srp[i] = __ldg(rowptr + RA + i);
@@ -257,7 +260,8 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         auto rp = [&](int r) -> int { return fits ? srp[r - RA] : __ldg(rowptr + r); };
 
         // ---- this lane's chunk ------------------------------------------
-        const int c0 = lane * S;
+        const int c0 = lane * S;            // first nonzero of the chunk in the unit
+        const int cs0 = lane * (S + 1);     // its place in the staged col and val
         const int cnt = max(0, min(S, cntu - c0));
         const int s0 = U0 + c0, send = s0 + cnt;
         double xs[K == 1 ? S : 1];       // K == 1: every gather issued up front
@@ -266,9 +270,9 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             if constexpr (K == 1) {
 #pragma unroll
                 for (int j = 0; j < S; ++j)
-                    xs[j] = ptx::ldg_x_issue(x + (long long)scol[c0 + (j < cnt ? j : 0)] * ldx, pol_x);
+                    xs[j] = ptx::ldg_x_issue(x + (long long)scol[cs0 + (j < cnt ? j : 0)] * ldx, pol_x);
             } else {
-                gather_row<K>(x, scol[c0], ldx, cur, pol_x);
+                gather_row<K>(x, scol[cs0], ldx, cur, pol_x);
             }
         }
         int r0 = RA, rl = RA;
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         int hrow = -1, trow = -1;
 
         auto fma_row = [&](int j, const double (&xr)[K]) {
-            const double v = value_at<VK>(sval + c0 + j);
+            const double v = value_at<VK>(sval + cs0 + j);
 #pragma unroll
             for (int c = 0; c < K; ++c) {
                 if constexpr (VK == VAL_PATTERN) acc[c] += xr[c];
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                 fma_row(j, xr);
             } else {
                 double nxt[K];
-                if (j + 1 < cnt) gather_row<K>(x, scol[c0 + j + 1], ldx, nxt, pol_x);
+                if (j + 1 < cnt) gather_row<K>(x, scol[cs0 + j + 1], ldx, nxt, pol_x);
                 fma_row(j, cur);
 #pragma unroll
                 for (int c = 0; c < K; ++c) cur[c] = nxt[c];

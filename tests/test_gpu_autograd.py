@@ -38,6 +38,13 @@ def test_transpose_structure_matches_scipy(sblas_lib, cuda):
     np.testing.assert_array_equal(t_rp.cpu().numpy(), at.indptr)
     np.testing.assert_array_equal(t_c.cpu().numpy(), at.indices)
     np.testing.assert_array_equal(v[perm.cpu().numpy()], at.data)
+    # the values of A^T gathered on the device, FP64 and FP32
+    for dt in (torch.float64, torch.float32):
+        src = a.val.to(dt)
+        out = torch.empty_like(src)
+        ops.gather_values(src, perm, out)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), src.cpu().numpy()[perm.cpu().numpy()])
 
 
 @pytest.mark.parametrize("k", [1, 4, 16])
