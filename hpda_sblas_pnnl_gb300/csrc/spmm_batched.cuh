@@ -303,6 +303,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
 #pragma unroll
         for (int c = 0; c < K; ++c) acc[c] = 0.0;
         bool has_head = false, has_tail = false, mid_lane = false;
+        bool noemit = false;   // the chunk ends no row
         int hrow = -1, trow = -1;
 
         auto fma_row = [&](int j, const double (&xr)[K]) {
@@ -348,6 +349,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             has_tail = !ends;
             trow = rl;
             mid_lane = has_tail && sb && mask == 0u;
+            noemit = mask == 0u && !ends;
         } else if (cnt > 0) {
             // general path: empty rows inside the chunk, or more rows than
             // the row buffer holds (rows then go straight to y)
@@ -392,6 +394,41 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                 has_tail = true;
                 trow = r;
                 mid_lane = first && sb;
+                noemit = first;
+            }
+        }
+
+        // ---- a unit inside one row that continues past it (every chunk full,
+        // none ending a row): its total is the unit's tail carry, summed over
+        // the lanes by a reduce-scatter butterfly (K - 1 + 5 - log2 K adds per
+        // lane instead of the segmented scan's 5 K)
+        if constexpr (K >= 2) {
+            if (__all_sync(FULL, cnt == S && noemit)) {
+                constexpr int LK = K == 2 ? 1 : K == 4 ? 2 : K == 8 ? 3 : 4;
+                double v[K];
+#pragma unroll
+                for (int c = 0; c < K; ++c) v[c] = acc[c];
+#pragma unroll
+                for (int st = 0; st < LK; ++st) {
+                    const int d = 16 >> st;
+                    const int h = K >> (st + 1);
+                    const bool up = (lane & d) != 0;
+#pragma unroll
+                    for (int i = 0; i < h; ++i) {
+                        const double mine = up ? v[i + h] : v[i];
+                        const double other = up ? v[i] : v[i + h];
+                        v[i] = mine + __shfl_xor_sync(FULL, other, d);
+                    }
+                }
+#pragma unroll
+                for (int st = LK; st < 5; ++st) v[0] += __shfl_xor_sync(FULL, v[0], 16 >> st);
+                if ((lane & ((1 << (5 - LK)) - 1)) == 0)
+                    a.tail_val[(long long)u * K + (lane >> (5 - LK))] = v[0];
+                if (lane == 0) {
+                    a.tail_row[u] = trow;
+                    a.head_row[u] = -1;
+                }
+                continue;   // no row of Y is finished in this unit
             }
         }
 
