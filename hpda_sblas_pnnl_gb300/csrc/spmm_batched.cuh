@@ -439,7 +439,27 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         if (!has_tail) trow = -1;
         const int trow_prev = __shfl_up_sync(FULL, trow, 1);
         const bool cont = mid_lane && lane > 0 && trow_prev == trow;
-        if (__any_sync(FULL, cont)) {
+        const unsigned contm = __ballot_sync(FULL, cont);
+        // run length: the consecutive lanes whose tails continue into this one
+        const unsigned starts = ~contm & ((2u << lane) - 1u);
+        const int lrun = contm ? lane - (31 - __clz(starts)) : 0;
+        const int maxrun = contm ? __reduce_max_sync(FULL, (unsigned)lrun) : 0;
+        if (maxrun > 0 && maxrun <= 3) {
+            // short runs (the common case): add the few tails before each
+            // lane directly, maxrun * K adds instead of the scan's 5 K
+            double base[K];
+#pragma unroll
+            for (int c = 0; c < K; ++c) base[c] = sv[c];
+#pragma unroll
+            for (int d = 1; d <= 3; ++d) {
+                if (d > maxrun) break;
+#pragma unroll
+                for (int c = 0; c < K; ++c) {
+                    const double so = __shfl_up_sync(FULL, base[c], d);
+                    sv[c] += (d <= lrun) ? so : 0.0;
+                }
+            }
+        } else if (maxrun > 3) {
             bool f = !cont;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
