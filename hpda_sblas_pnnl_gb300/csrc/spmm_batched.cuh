@@ -14,8 +14,10 @@
 //   - a row that starts and ends inside one lane's chunk goes to the warp's
 //     row buffer in shared memory;
 //   - a row crossing lanes: each lane keeps its last partial (tail) and its
-//     first segment (head); a segmented shuffle scan over the tails joins
-//     them (run only when some row spans three or more lanes);
+//     first segment (head); the tails of a run of lanes are joined by direct
+//     adds when every run spans at most four lanes, else by a segmented
+//     shuffle scan; a unit lying inside one row is summed by a
+//     reduce-scatter butterfly instead;
 //   - a row crossing units: the unit's first-row partial (head) and
 //     last-row partial (tail) go to per-unit carry arrays, and the fix-up
 //     kernel adds, for every head, the tails of the preceding units of the
@@ -23,7 +25,11 @@
 //   - the unit's completed rows are written out by the whole warp at the
 //     end (coalesced), alpha and beta applied once per row and column.
 // Units with more rows than the row buffer holds, or with empty rows inside
-// a chunk, take a per-lane general path with the same results.
+// a chunk, take a per-lane general path with the same results.  Staged col
+// and val sit at an odd per-lane stride (S + 1) so the lanes' strided
+// shared-memory reads do not collide in a bank.  Matrices may list the rows
+// of Y their stored rows write (row_ids) and read their values through a
+// permutation (val_perm): the transposed operator of the adjoint uses both.
 #pragma once
 
 #include <climits>
