@@ -53,6 +53,18 @@ class BatchMatrix(C.Structure):
     ]
 
 
+class MMHeader(C.Structure):
+    """include/mmio.h (sblas_mm_header): banner and size line of a file."""
+
+    _fields_ = [
+        ("m", C.c_int),
+        ("n", C.c_int),
+        ("nnz", C.c_longlong),
+        ("typecode", C.c_char * 4),
+        ("reserved", C.c_int),
+    ]
+
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
@@ -142,6 +154,15 @@ SIGNATURES: dict[str, tuple] = {
     "print_vec_int": (None, [_ip, C.c_int, C.c_char_p]),
     "print_vec_gpu_double": (None, [_dp, C.c_int, C.c_char_p]),
     "print_vec_gpu_int": (None, [_ip, C.c_int, C.c_char_p]),
+    # include/mmio.h (FILE * and MM_typecode passed as plain pointers)
+    "mm_read_banner": (C.c_int, [_vp, _vp]),
+    "mm_read_mtx_crd_size": (C.c_int, [_vp, _ip, _ip, _ip]),
+    "mm_read_mtx_array_size": (C.c_int, [_vp, _ip, _ip]),
+    "mm_is_valid": (C.c_int, [C.c_char_p]),
+    "mm_typecode_to_str": (_vp, [C.c_char_p]),
+    "sblas_mm_read_header": (C.c_int, [C.c_char_p, C.POINTER(MMHeader)]),
+    "sblas_mm_read_coo": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_longlong, _vp, _vp, _vp,
+                                    C.POINTER(C.c_longlong)]),
 }
 
 

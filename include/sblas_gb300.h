@@ -37,6 +37,7 @@ extern "C" {
 #define SBLAS_ERR_ALIGN (-5)          /* device array not 16-byte aligned */
 #define SBLAS_ERR_KERNEL (-6)         /* a kernel reported a device-side error */
 #define SBLAS_ERR_UNSUPPORTED (-7)    /* option not compiled in this build */
+#define SBLAS_ERR_FORMAT (-8)         /* malformed input file (MatrixMarket reader) */
 
 /* kernel versions, numbered as the reference's `kernel` argument
  * (src/dspmv_mgpu_v1.cu:256-278) */
