@@ -116,6 +116,9 @@ SIGNATURES: dict[str, tuple] = {
                                       _vp, C.c_size_t, _vp]),
     "sblas_gather_values": (C.c_int, [C.c_longlong, C.c_int, _vp, _vp, _vp, _vp]),
     "sblas_zero": (C.c_int, [_vp, C.c_size_t, _vp]),
+    "sblas_csr_filter_x_workspace_bytes": (C.c_size_t, [C.c_longlong]),
+    "sblas_csr_filter_x": (C.c_int, [C.c_int, C.c_longlong, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, C.c_size_t, _vp]),
     # include/spmv_kernel.h (reference signatures)
     "csr5_kernel": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _vp, _vp, _vp, _dp, _vp, _vp]),
     "spMV_mgpu_baseline": (SpmvRet, [C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp,

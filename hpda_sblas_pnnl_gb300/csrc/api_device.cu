@@ -291,6 +291,26 @@ int sblas_gather_values(long long nnz, int val_kind, const void *src, const int 
     return launch_gather_values(nnz, val_kind, src, perm, dst, static_cast<cudaStream_t>(stream));
 }
 
+size_t sblas_csr_filter_x_workspace_bytes(long long nnz)
+{
+    return csr_filter_x_workspace_bytes(nnz);
+}
+
+int sblas_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
+                       const double *val, const double *x, int *out_rowptr, int *out_col,
+                       double *out_val, void *work, size_t work_bytes, void *stream)
+{
+    clear_error();
+    if (rowptr == nullptr || out_rowptr == nullptr ||
+        (nnz > 0 && (col == nullptr || x == nullptr || out_col == nullptr ||
+                     (val == nullptr) != (out_val == nullptr)))) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_csr_filter_x(m, nnz, rowptr, col, val, x, out_rowptr, out_col, out_val, work,
+                               work_bytes, static_cast<cudaStream_t>(stream));
+}
+
 int sblas_zero(void *p, size_t bytes, void *stream)
 {
     clear_error();

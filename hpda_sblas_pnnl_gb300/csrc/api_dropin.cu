@@ -10,10 +10,12 @@
 // staging copy on a one-GPU, one-NUMA-node process).
 #include <sys/time.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/spmv_kernel.h"
@@ -541,6 +543,61 @@ spmv_ret spMV_mgpu_v1_numa_coo(int m, int n, int nnz, double *alpha, double *coo
 
 // SpMSpV: the nonzeros whose x entry is zero are dropped on the host before
 // the SpMV, as src/dspmv_mgpu_v1.cu:19-74 does.
+// spMspV's x-zero filter (src/dspmv_mgpu_v1.cu:29-40) on all host threads:
+// the rows are cut into blocks of about equal nonzeros, every block counts
+// its kept nonzeros, an exclusive prefix of the counts gives every block its
+// output offset, and every block then writes its rows.  The output equals
+// the reference's serial loop.
+static void host_filter_x(int m, const int *rowptr, const int *col, const double *val,
+                          const double *x, std::vector<int> &rp, std::vector<int> &rc,
+                          std::vector<double> &rv)
+{
+    const long long nnz = (long long)rowptr[m] - rowptr[0];
+    int T = (int)std::thread::hardware_concurrency();
+    T = std::max(1, std::min(T, 64));
+    if (nnz < (1LL << 20)) T = 1;
+    std::vector<int> rb(T + 1);
+    rb[0] = 0;
+    rb[T] = m;
+    for (int t = 1; t < T; ++t) {
+        const long long target = rowptr[0] + nnz * t / T;
+        const int r = (int)(std::upper_bound(rowptr, rowptr + m + 1, (int)target) - rowptr) - 1;
+        rb[t] = std::min(m, std::max(rb[t - 1], r));
+    }
+    std::vector<long long> first(T + 1, 0);
+    auto run = [&](auto &&body) {
+        if (T == 1) {
+            body(0);
+            return;
+        }
+        std::vector<std::thread> th;
+        th.reserve(T);
+        for (int t = 0; t < T; ++t) th.emplace_back(body, t);
+        for (auto &h : th) h.join();
+    };
+    run([&](int t) {
+        long long c = 0;
+        for (int j = rowptr[rb[t]]; j < rowptr[rb[t + 1]]; ++j) c += (x[col[j]] != 0.0);
+        first[t + 1] = c;
+    });
+    for (int t = 0; t < T; ++t) first[t + 1] += first[t];
+    rp.assign((size_t)m + 1, 0);
+    rc.resize((size_t)first[T]);
+    rv.resize((size_t)first[T]);
+    run([&](int t) {
+        long long k = first[t];
+        for (int i = rb[t]; i < rb[t + 1]; ++i) {
+            for (int j = rowptr[i]; j < rowptr[i + 1]; ++j)
+                if (x[col[j]] != 0.0) {
+                    rc[(size_t)k] = col[j];
+                    rv[(size_t)k] = val[j];
+                    ++k;
+                }
+            rp[(size_t)i + 1] = (int)k;
+        }
+    });
+}
+
 static spmv_ret spmspv(const char *name, int m, int n, int nnz, double *alpha, double *val,
                        int *rowptr, int *col, double *x, double *beta, double *y, int ngpu,
                        int kernel, int v2, int nb, int q)
@@ -551,18 +608,8 @@ static spmv_ret spmspv(const char *name, int m, int n, int nnz, double *alpha, d
         return failed();
     const double t0 = wall();
     std::vector<double> rv;
-    std::vector<int> rc, rp((size_t)m + 1);
-    rv.reserve(nnz);
-    rc.reserve(nnz);
-    rp[0] = 0;
-    for (int i = 0; i < m; ++i) {
-        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j)
-            if (x[col[j]] != 0.0) {
-                rv.push_back(val[j]);
-                rc.push_back(col[j]);
-            }
-        rp[i + 1] = (int)rv.size();
-    }
+    std::vector<int> rc, rp;
+    host_filter_x(m, rowptr, col, val, x, rp, rc, rv);
     const double filt = wall() - t0;
     spmv_ret r = v2 ? spMV_mgpu_v2(m, n, (int)rv.size(), alpha, rv.data(), rp.data(), rc.data(),
                                    x, beta, y, ngpu, kernel, nb, q)

@@ -9,8 +9,12 @@
 //     pointer entries of the rows in between);
 //   * CSC -> CSR: a stable radix sort of (row, CSC position) pairs (CUB,
 //     part of the CUDA toolkit), then a gather of column and value; stability
-//     keeps columns ascending inside each row, as cuSPARSE's stable coosort.
+//     keeps columns ascending inside each row, as cuSPARSE's stable coosort;
+//   * spMspV's x-zero filter: a keep flag per nonzero, an exclusive scan of
+//     the flags (CUB) giving every kept nonzero its output position and every
+//     row its new row pointer, then a scatter.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "sblas_internal.h"
 
@@ -287,6 +291,84 @@ int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
 {
     if (nnz <= 0) return SBLAS_OK;
     gather_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, perm, in_i, out_i, in_d, out_d);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
+namespace {
+__global__ void filter_flags_kernel(long long nnz, const int *__restrict__ col,
+                                    const double *__restrict__ x, int *__restrict__ flag)
+{
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j <= nnz;
+         j += (long long)gridDim.x * blockDim.x)
+        flag[j] = (j < nnz && __ldg(x + __ldg(col + j)) != 0.0) ? 1 : 0;
+}
+
+__global__ void filter_scatter_kernel(long long nnz, const int *__restrict__ col,
+                                      const double *__restrict__ val,
+                                      const int *__restrict__ flag, const int *__restrict__ pos,
+                                      int *__restrict__ ocol, double *__restrict__ oval)
+{
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nnz;
+         j += (long long)gridDim.x * blockDim.x)
+        if (flag[j]) {
+            const int q = pos[j];
+            ocol[q] = __ldg(col + j);
+            if (val) oval[q] = __ldg(val + j);
+        }
+}
+
+__global__ void filter_rowptr_kernel(int m, const int *__restrict__ rowptr,
+                                     const int *__restrict__ pos, int *__restrict__ orowptr)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= m;
+         i += (long long)gridDim.x * blockDim.x)
+        orowptr[i] = pos[__ldg(rowptr + i)];
+}
+
+size_t filter_cub_bytes(long long nnz)
+{
+    size_t cub_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (const int *)nullptr, (int *)nullptr,
+                                  (int)(nnz + 1));
+    return cub_bytes;
+}
+}  // namespace
+
+size_t csr_filter_x_workspace_bytes(long long nnz)
+{
+    if (nnz < 0) nnz = 0;
+    return al256(filter_cub_bytes(nnz)) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
+}
+
+int launch_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
+                        const double *val, const double *x, int *orowptr, int *ocol,
+                        double *oval, void *work, size_t work_bytes, cudaStream_t stream)
+{
+    if (m < 0 || nnz < 0 || nnz >= 0x7fffffffLL) {
+        set_error(SBLAS_ERR_ARG, "bad sizes m=%d nnz=%lld", m, nnz);
+        return SBLAS_ERR_ARG;
+    }
+    const size_t cub_bytes = filter_cub_bytes(nnz);
+    const size_t need = al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
+    if (work == nullptr || work_bytes < need) {
+        set_error(SBLAS_ERR_ARG, "csr_filter_x workspace too small (%zu < %zu)", work_bytes, need);
+        return SBLAS_ERR_ARG;
+    }
+    unsigned char *w = static_cast<unsigned char *>(work);
+    int *flag = reinterpret_cast<int *>(w + al256(cub_bytes));
+    int *pos = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * (nnz + 1)));
+    filter_flags_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(nnz, col, x, flag);
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    size_t cb = cub_bytes;
+    SBLAS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w, cb, flag, pos, (int)(nnz + 1), stream));
+    if (nnz > 0) {
+        filter_scatter_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, col, val, flag, pos,
+                                                                      ocol, oval);
+        SBLAS_CUDA_TRY(cudaGetLastError());
+    }
+    filter_rowptr_kernel<<<grid_for((long long)m + 1, 256), 256, 0, stream>>>(m, rowptr, pos,
+                                                                             orowptr);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }

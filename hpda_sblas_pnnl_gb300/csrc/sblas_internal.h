@@ -80,6 +80,11 @@ int launch_csr_transpose(int m, int n, long long nnz, const int *rowptr, const i
                          cudaStream_t stream);
 int launch_gather_values(long long nnz, int val_kind, const void *src, const int *perm, void *dst,
                          cudaStream_t stream);
+// spMspV's x-zero filter: CSR of the nonzeros with x[col] != 0.
+size_t csr_filter_x_workspace_bytes(long long nnz);
+int launch_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
+                        const double *val, const double *x, int *orowptr, int *ocol,
+                        double *oval, void *work, size_t work_bytes, cudaStream_t stream);
 int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
                       const int *csc_colptr, const int *csc_row, double *csr_val,
                       int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,

@@ -367,3 +367,38 @@ def gather_values(val: torch.Tensor, perm: torch.Tensor, out: torch.Tensor) -> t
                                          _ptr(out), _stream_ptr(dev))
     _lib.check(rc)
     return out
+
+
+def csr_filter_x(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
+                 x: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor | None]:
+    """spMspV's x-zero filter on the device (src/dspmv_mgpu_v1.cu:29-40): the
+    CSR matrix of the nonzeros whose x[col] != 0, in storage order.  Reads the
+    kept count back (one synchronisation) to size the outputs."""
+    dev = _require_cuda(rowptr, col, val, x)
+    if val is not None and val.dtype != torch.float64:
+        raise TypeError("val must be float64 or None")
+    m = rowptr.numel() - 1
+    nnz = col.numel()
+    lib = _lib.load()
+    wb = int(lib.sblas_csr_filter_x_workspace_bytes(nnz))
+    work = torch.empty(max(wb, 1), dtype=torch.uint8, device=dev)
+    orp = torch.empty(m + 1, dtype=torch.int32, device=dev)
+    ocol = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    oval = None if val is None else torch.empty(max(nnz, 1), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        rc = lib.sblas_csr_filter_x(m, nnz, _ptr(rowptr), _ptr(col), _ptr(val), _ptr(x),
+                                    _ptr(orp), _ptr(ocol), _ptr(oval), _ptr(work), wb,
+                                    _stream_ptr(dev))
+    _lib.check(rc)
+    k = int(orp[m].item())
+    return orp, ocol[:k], (None if oval is None else oval[:k])
+
+
+def spmspv(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, x: torch.Tensor,
+           y: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+           kernel: int = KERNEL_MERGEPATH) -> torch.Tensor:
+    """y = alpha*A'*x + beta*y with A' = A without the nonzeros whose x entry
+    is zero, as spMspV_mgpu_v1 computes it (src/dspmv_mgpu_v1.cu:19-74), on
+    device arrays: the filter and the product both run on the GPU."""
+    orp, ocol, oval = csr_filter_x(rowptr, col, val, x)
+    return csrmv(orp, ocol, oval, x, y, alpha, beta, n=x.numel(), kernel=kernel)

@@ -225,6 +225,17 @@ SBLAS_API size_t sblas_csr_transpose_workspace_bytes(int m, int n, long long nnz
 SBLAS_API int sblas_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
                                   int *t_rowptr, int *t_col, int *perm, void *work,
                                   size_t work_bytes, void *stream);
+/* The x-zero filter of spMspV_mgpu_v1 / _v2 (src/dspmv_mgpu_v1.cu:29-40),
+ * on the device: the nonzeros j with x[col[j]] != 0.0, in storage order, as
+ * a CSR matrix out_rowptr[m + 1] (out_rowptr[m] = the kept count),
+ * out_col / out_val (room for nnz entries).  val and out_val may both be
+ * NULL (pattern).  rowptr[0] must be 0.  Asynchronous on stream; work:
+ * sblas_csr_filter_x_workspace_bytes. */
+SBLAS_API size_t sblas_csr_filter_x_workspace_bytes(long long nnz);
+SBLAS_API int sblas_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
+                                 const double *val, const double *x, int *out_rowptr,
+                                 int *out_col, double *out_val, void *work, size_t work_bytes,
+                                 void *stream);
 /* dst[p] = src[perm[p]] for nnz values of the given kind (FP64 or FP32). */
 SBLAS_API int sblas_gather_values(long long nnz, int val_kind, const void *src, const int *perm,
                                   void *dst, void *stream);

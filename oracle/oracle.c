@@ -363,3 +363,23 @@ void oracle_csr_sddmm(int m, int k, const int *rowptr, const int *col, const dou
             dval[p] = s;
         }
 }
+
+/* The x-zero filter of spMspV_mgpu_v1 / _v2 (src/dspmv_mgpu_v1.cu:29-40,
+ * src/dspmv_mgpu_v2.cu:55-65): keep the nonzeros j of every row with
+ * x[col[j]] != 0.0, in storage order; returns the kept count. */
+long long oracle_csr_filter_x(int m, const int *rowptr, const int *col, const double *val,
+                              const double *x, int *orowptr, int *ocol, double *oval)
+{
+    long long k = 0;
+    orowptr[0] = 0;
+    for (int i = 0; i < m; i++) {
+        for (int j = rowptr[i]; j < rowptr[i + 1]; j++)
+            if (x[col[j]] != 0.0) {
+                oval[k] = val[j];
+                ocol[k] = col[j];
+                k++;
+            }
+        orowptr[i + 1] = (int)k;
+    }
+    return k;
+}

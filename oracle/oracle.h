@@ -49,6 +49,8 @@ void oracle_csr_spmm_t(int m, int n, int k, const double *val, const int *rowptr
                        const int *col, const double *g, int ldg, double *dx, int lddx);
 void oracle_csr_sddmm(int m, int k, const int *rowptr, const int *col, const double *g, int ldg,
                       const double *x, int ldx, double *dval);
+long long oracle_csr_filter_x(int m, const int *rowptr, const int *col, const double *val,
+                              const double *x, int *orowptr, int *ocol, double *oval);
 
 #ifdef __cplusplus
 }

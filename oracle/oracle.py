@@ -54,6 +54,8 @@ def _lib() -> C.CDLL:
                                          _dp, C.c_int]
         _o.oracle_csr_sddmm.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, _dp, C.c_int,
                                         _dp]
+        _o.oracle_csr_filter_x.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _ip, _ip, _dp]
+        _o.oracle_csr_filter_x.restype = C.c_longlong
     return _o
 
 
@@ -202,6 +204,17 @@ def coo2csr(m, n, val, row, col):
     c = np.empty(nnz, np.int32)
     _lib().oracle_coo2csr(m, n, nnz, _d(val), _i(row), _i(col), _d(v), _i(p), _i(c))
     return v, p, c
+
+
+def csr_filter_x(m, rowptr, col, val, x):
+    """(rowptr, col, val) of the nonzeros whose x[col] != 0 (spMspV's filter)."""
+    nnz = int(col.size)
+    orp = np.empty(m + 1, np.int32)
+    oc = np.empty(max(nnz, 1), np.int32)
+    ov = np.empty(max(nnz, 1), np.float64)
+    k = _lib().oracle_csr_filter_x(m, _i(rowptr), _i(col), _d(val), _d(x), _i(orp), _i(oc),
+                                   _d(ov))
+    return orp, oc[:k].copy(), ov[:k].copy()
 
 
 def coo2csc(m, n, val, row, col):

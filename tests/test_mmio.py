@@ -200,7 +200,7 @@ def test_file_to_csr_to_spmv(sblas_lib, cuda, tmp_path):
     p = write(tmp_path, "g.mtx", BANNER.format("real", "general") + f"{m} {n} {nz}\n" +
               "".join(f"{a} {b} {float(x)!r}\n" for a, b, x in zip(r, c, v)))
     mm, nn, rp, col, val = mmio.read_csr(p)
-    _, _, orow, ocol, oval = R.read_coo(p)
+    _, _, _, orow, ocol, oval = R.read_coo(p)
     ov, op_, oc = O.coo2csr(m, n, oval, orow, ocol)
     np.testing.assert_array_equal(rp, op_)
     np.testing.assert_array_equal(col, oc)

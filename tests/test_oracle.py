@@ -154,3 +154,26 @@ def test_oracle_spmm_and_adjoints_match_scipy():
     y1 = rng.standard_normal(300)
     np.testing.assert_array_equal(O.csr_spmm(300, 200, rp, c, v, x1, y1, 2.0, 0.5),
                                   O.csr_spmv(300, 200, rp, c, v, x1, y1, 2.0, 0.5))
+
+
+def test_oracle_filter_x_matches_numpy_and_leaves_finite_products_unchanged():
+    """spMspV's filter (src/dspmv_mgpu_v1.cu:29-40): kept nonzeros in storage
+    order; with finite values the filtered product equals the unfiltered one
+    bit for bit (the dropped terms are signed zeros added to a sum)."""
+    rng = np.random.default_rng(12)
+    a = sp.random(3000, 2000, density=0.01, format="csr", random_state=12)
+    a.data = rng.standard_normal(a.nnz)
+    rp, col, val = a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data
+    x = rng.uniform(-1, 1, 2000)
+    x[rng.random(2000) < 0.7] = 0.0
+    x[rng.random(2000) < 0.05] = -0.0
+    orp, oc, ov = O.csr_filter_x(3000, rp, col, val, x)
+    keep = x[col] != 0.0
+    np.testing.assert_array_equal(oc, col[keep])
+    np.testing.assert_array_equal(ov, val[keep])
+    rows = np.repeat(np.arange(3000), np.diff(rp))
+    np.testing.assert_array_equal(orp, np.concatenate([[0], np.cumsum(np.bincount(
+        rows[keep], minlength=3000))]))
+    full = O.csr_spmv(3000, 2000, rp, col, val, x, np.zeros(3000))
+    filt = O.csr_spmv(3000, 2000, orp, oc, ov, x, np.zeros(3000))
+    assert full.tobytes() == filt.tobytes()
