@@ -58,6 +58,11 @@ def parse():
     p.add_argument("--kernel-only", action="store_true",
                    help="time the device steps only (no e2e, CPU baseline, extras): the "
                         "small case used for ncu captures")
+    p.add_argument("--matrix", default="powerlaw", choices=["powerlaw", "banded"],
+                   help="with --kernel-only: the matrix of the profiled case (banded: the "
+                        "FEM-like generator, --m rows)")
+    p.add_argument("--values", default="f64", choices=["f64", "f32"],
+                   help="with --kernel-only: FP64 values or FP32 values (FP64 sums)")
     return p.parse_args()
 
 
@@ -236,10 +241,15 @@ def run_ours(args):
 
     # each rank holds its own full-size instance (weak scaling, no collective
     # on the data path): rank r uses seed + r
-    a, x = make_workload(dev, args.seed + rank, args.m)
+    if args.kernel_only and args.matrix == "banded":
+        a, x = synth.banded_fem(m=args.m, seed=args.seed + rank, device=dev)
+    else:
+        a, x = make_workload(dev, args.seed + rank, args.m)
+    if args.kernel_only and args.values == "f32":
+        a.val = a.val.float()
     m, n, nnz = a.m, a.n, a.nnz
     y = torch.zeros(m, dtype=torch.float64, device=dev)
-    bytes_step = synth.compulsory_bytes(m, n, nnz)
+    bytes_step = synth.compulsory_bytes(m, n, nnz, val_bytes=a.val.element_size())
     kernel = ops.KERNEL_MERGEPATH
     # tile shape: --sigma, else the library default for --kernel-only (the
     # profiling case), else the autotuner's measured pick on this matrix
@@ -282,16 +292,17 @@ def run_ours(args):
     launches_per_step = 3
 
     # correctness of what was timed (oracle spot check on rank 0 is in the
-    # tests; here a cheap invariant: values are 1.0, so sum(y) = sum colcount*x)
-    cc = torch.bincount(a.col.to(torch.int64), minlength=n).to(torch.float64)
-    chk = abs(float(y.sum()) - float((cc * x).sum())) / float((cc * x).sum())
+    # tests; here a cheap invariant: sum(y) = sum over nonzeros of val * x[col])
+    tot = float((a.val.double() * x[a.col.to(torch.int64)]).sum())
+    chk = abs(float(y.sum()) - tot) / max(abs(tot), 1e-300)
 
     out = {}
     if rank == 0 and args.kernel_only:
         print(json.dumps({"metric": METRIC, "value": round(value, 2), "unit": "GB/s",
                           "n_gpus": ws, "steps": args.steps, "ms_per_step": round(ms_step, 4),
-                          "config": {"m": m, "nnz": nnz, "sigma": sigma,
-                                     "bytes_per_step": bytes_step},
+                          "config": {"matrix": args.matrix, "values": args.values, "m": m,
+                                     "nnz": nnz, "sigma": sigma, "bytes_per_step": bytes_step,
+                                     "check_rel_err": chk},
                           "note": "kernel-only small case (profiling); not the benchmark line"}),
               flush=True)
     elif rank == 0:
