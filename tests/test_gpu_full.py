@@ -132,3 +132,61 @@ def test_host_entry_point_overlapped_chunks(sblas_lib, cuda, kernel):
         y = arr(np.full(a.m, np.nan))
         api.spMV_mgpu_baseline(a.m, a.n, a.nnz, 1.0, arr(v), arr(rp), arr(c), arr(xx), 0.0, y)
         assert rel_l2(y, O.csr_spmv(a.m, a.n, rp, c, v, xx, np.zeros(a.m), threads=THREADS)) <= 1e-12
+
+
+def test_nnz_at_the_int32_limit(sblas_lib, cuda):
+    """Maximum size: 2,147,000,000 nonzeros (int32 row pointers hold at most
+    2^31 - 1), 16M rows of 0 to 268 nonzeros (rowptr[i] = floor((i/m)^2 nnz):
+    empty rows first).  Values 1, 2, 3 in turn and x in {1, ..., 4}: every
+    product and row sum is an integer below 2^53, so the exact y is known in
+    any summation order and every kernel (1, 2, 3, the pattern form and the
+    batched plan) must match it bit for bit.  About 32 GB on the device."""
+    from hpda_sblas_pnnl_gb300 import ops
+    nnz, m, n = 2_147_000_000, 16_000_000, 16_000_000
+    g = torch.Generator(device=cuda)
+    g.manual_seed(31)
+    i = torch.arange(m + 1, dtype=torch.float64, device=cuda)
+    rp64 = torch.floor((i / m) ** 2 * nnz).to(torch.int64)
+    rp64[-1] = nnz
+    del i
+    rowptr = rp64.to(torch.int32)
+    col = torch.randint(0, n, (nnz,), generator=g, dtype=torch.int32, device=cuda)
+    val = torch.empty(nnz, dtype=torch.float64, device=cuda)
+    step = 1 << 28
+    for s in range(0, nnz, step):
+        e = min(nnz, s + step)
+        val[s:e] = (torch.arange(s, e, device=cuda) % 3 + 1).to(torch.float64)
+    x = torch.randint(1, 5, (n,), generator=g, device=cuda).to(torch.float64)
+    # exact results by row blocks: prefix sums of the products
+    want = torch.empty(m, dtype=torch.float64, device=cuda)
+    want_pat = torch.empty(m, dtype=torch.float64, device=cuda)
+    rb = 1 << 20
+    for r0 in range(0, m, rb):
+        r1 = min(m, r0 + rb)
+        j0, j1 = int(rp64[r0]), int(rp64[r1])
+        xg = x[col[j0:j1].long()]
+        lo, hi = rp64[r0:r1] - j0, rp64[r0 + 1:r1 + 1] - j0
+        for out, terms in ((want, val[j0:j1] * xg), (want_pat, xg)):
+            pre = torch.zeros(j1 - j0 + 1, dtype=torch.float64, device=cuda)
+            torch.cumsum(terms, 0, out=pre[1:])
+            out[r0:r1] = pre[hi] - pre[lo]
+            del pre
+        del xg, lo, hi
+    assert float(want.max()) < 2.0 ** 53
+    y = torch.empty(m, dtype=torch.float64, device=cuda)
+    for kernel in (1, 2, 3):
+        y.fill_(float("nan"))
+        ops.csrmv(rowptr, col, val, x, y, 1.0, 0.0, n=n, kernel=kernel)
+        torch.cuda.synchronize()
+        assert torch.equal(y, want), kernel
+    y.fill_(float("nan"))
+    ops.csrmv(rowptr, col, None, x, y, 1.0, 0.0, n=n)
+    torch.cuda.synchronize()
+    assert torch.equal(y, want_pat)
+    y.fill_(float("nan"))
+    plan = ops.SpmmPlan(rowptr, col, val, n=n, k=1)
+    plan(x, y)
+    torch.cuda.synchronize()
+    assert torch.equal(y, want)
+    del plan, col, val, rowptr, rp64, want, want_pat, y, x
+    torch.cuda.empty_cache()
