@@ -635,6 +635,14 @@ def run_probe():
     for rng in (4_000_000, 250_000, 16_384):
         _lib.check(lib.sblas_probe_gather(rng, C.byref(gps)))
         out[f"random_8B_gathers_per_s_range_{rng}"] = gps.value
+    # shared memory reserved per CTA (256 threads): the split of the SM's
+    # 256 KB between shared memory and L1 that the driver picks for the launch
+    occ = C.c_int()
+    sweep = {}
+    for kb in (0, 16, 24, 32, 40, 48, 56, 80, 100):
+        _lib.check(lib.sblas_probe_gather_smem(4_000_000, kb * 1024, C.byref(gps), C.byref(occ)))
+        sweep[f"{kb}KB_x{occ.value}"] = gps.value
+    out["random_8B_gathers_per_s_by_smem_per_cta_x_ctas_per_sm"] = sweep
     _lib.check(lib.sblas_probe_stream(C.byref(bps)))
     out["hbm_read_bytes_per_s"] = bps.value
     print(json.dumps(out), flush=True)

@@ -94,6 +94,7 @@ SIGNATURES: dict[str, tuple] = {
                                        C.c_double, _vp, _vp]),
     "sblas_probe_fp64": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "sblas_probe_gather": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "sblas_probe_gather_smem": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double), _ip]),
     "sblas_probe_stream": (C.c_int, [C.POINTER(C.c_double)]),
     "sblas_dcoomv": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, _vp, _vp, _vp,
                                C.c_double, _vp, _vp, C.c_int, _vp, C.c_size_t, _vp]),

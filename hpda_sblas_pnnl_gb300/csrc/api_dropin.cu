@@ -276,8 +276,7 @@ spmv_ret run_host(Call c)
         set_error(SBLAS_ERR_ALLOC, "%s: device allocation failed", c.name);
         return failed();
     }
-    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1], e2 = ctx->ev[2], e3 = ctx->ev[3],
-                e4 = ctx->ev[4];
+    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1], e2 = ctx->ev[2], e3 = ctx->ev[3];
     // ---- host -> device
     DROPIN_CUDA(cudaEventRecord(e0, st));
     if (nnz > 0) {
@@ -360,7 +359,6 @@ spmv_ret run_host(Call c)
     DROPIN_CUDA(cudaEventElapsedTime(&t_comm, e0, e1));
     DROPIN_CUDA(cudaEventElapsedTime(&t_part, e1, e2));
     DROPIN_CUDA(cudaEventElapsedTime(&t_comp, e2, e3));
-    (void)e4;
 
     // ---- device -> host: only the rows this call writes
     const double tm = wall();

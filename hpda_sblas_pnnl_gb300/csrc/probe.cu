@@ -6,6 +6,8 @@
 //   sblas_probe_gather  random 8-byte loads from a vector resident in L2
 //                       (one per nonzero in CSR SpMV; each moves a 32-byte
 //                       sector from L2 to the SM)
+//   sblas_probe_gather_smem  the same with shared memory reserved per CTA (moves
+//                       the shared-memory / L1 split of the SM)
 //   sblas_probe_stream  streaming read bandwidth from HBM
 //
 // Diagnostics only (not on the SpMV path): they allocate and free their own
@@ -143,20 +145,35 @@ done:
     return rc;
 }
 
-int sblas_probe_gather(int range, double *gathers_per_s)
+int sblas_probe_gather_smem(int range, int smem_per_cta, double *gathers_per_s,
+                            int *ctas_per_sm)
 {
     clear_error();
-    if (range <= 0) {
-        set_error(SBLAS_ERR_ARG, "range must be positive");
+    if (range <= 0 || smem_per_cta < 0) {
+        set_error(SBLAS_ERR_ARG, "range must be positive, smem_per_cta not negative");
         return SBLAS_ERR_ARG;
     }
     int rc = SBLAS_OK;
     const long long n = 64LL << 20;
     const int sms = sms_now();
+    int occ = 0;
     double *x = nullptr, *out = nullptr;
     int *idx = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     float ms = 0.f;
+    // the dynamic shared memory is reserved, not used: it only moves the
+    // shared-memory / L1 split the driver picks for the launch
+    PROBE_TRY(cudaFuncSetAttribute(probe_gather_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem_per_cta));
+    PROBE_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, probe_gather_kernel, 256,
+                                                            (size_t)smem_per_cta));
+    if (occ < 1) {
+        set_error(SBLAS_ERR_ARG, "no CTA of 256 threads fits with %d bytes of shared memory",
+                  smem_per_cta);
+        rc = SBLAS_ERR_ARG;
+        goto done;
+    }
+    if (ctas_per_sm) *ctas_per_sm = occ;
     PROBE_TRY(cudaMalloc(&x, sizeof(double) * (size_t)range));
     PROBE_TRY(cudaMalloc(&idx, sizeof(int) * (size_t)n));
     PROBE_TRY(cudaMalloc(&out, sizeof(double)));
@@ -164,20 +181,26 @@ int sblas_probe_gather(int range, double *gathers_per_s)
     PROBE_TRY(cudaEventCreate(&e0));
     PROBE_TRY(cudaEventCreate(&e1));
     probe_fill_idx<<<sms * 8, 256>>>(idx, n, range);
-    probe_gather_kernel<<<sms * 8, 256>>>(x, idx, n, out);
+    probe_gather_kernel<<<sms * occ, 256, smem_per_cta>>>(x, idx, n, out);
     PROBE_TRY(cudaEventRecord(e0));
-    probe_gather_kernel<<<sms * 8, 256>>>(x, idx, n, out);
+    probe_gather_kernel<<<sms * occ, 256, smem_per_cta>>>(x, idx, n, out);
     PROBE_TRY(cudaEventRecord(e1));
     PROBE_TRY(cudaEventSynchronize(e1));
     PROBE_TRY(cudaEventElapsedTime(&ms, e0, e1));
     if (gathers_per_s) *gathers_per_s = (double)n / (ms * 1e-3);
 done:
+    cudaFuncSetAttribute(probe_gather_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 0);
     if (x) cudaFree(x);
     if (idx) cudaFree(idx);
     if (out) cudaFree(out);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return rc;
+}
+
+int sblas_probe_gather(int range, double *gathers_per_s)
+{
+    return sblas_probe_gather_smem(range, 0, gathers_per_s, nullptr);
 }
 
 int sblas_probe_stream(double *bytes_per_s)

@@ -132,6 +132,11 @@ SBLAS_API int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const do
  * streaming HBM read bytes per second. */
 SBLAS_API int sblas_probe_fp64(double *warp_instr_per_s_full, double *warp_instr_per_s_one_lane);
 SBLAS_API int sblas_probe_gather(int range, double *gathers_per_s);
+/* The gather probe with smem_per_cta bytes of (unused) shared memory per CTA
+ * of 256 threads and as many CTAs per SM as fit (*ctas_per_sm): shows how
+ * the shared-memory / L1 split the driver picks bounds random gathers. */
+SBLAS_API int sblas_probe_gather_smem(int range, int smem_per_cta, double *gathers_per_s,
+                                      int *ctas_per_sm);
 SBLAS_API int sblas_probe_stream(double *bytes_per_s);
 
 /* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
