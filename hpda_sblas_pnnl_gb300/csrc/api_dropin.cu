@@ -550,6 +550,12 @@ static void host_filter_x(int m, const int *rowptr, const int *col, const double
                           const double *x, std::vector<int> &rp, std::vector<int> &rc,
                           std::vector<double> &rv)
 {
+    if (m <= 0 || rowptr == nullptr) {   // no rows: an empty matrix (rowptr may be null)
+        rp.assign(1, 0);
+        rc.clear();
+        rv.clear();
+        return;
+    }
     const long long nnz = (long long)rowptr[m] - rowptr[0];
     int T = (int)std::thread::hardware_concurrency();
     T = std::max(1, std::min(T, 64));

@@ -149,6 +149,30 @@ def test_dropin_entry_points(sblas_lib, name, entry):
         assert_close(y, ref, exact=(name == "g200"))
 
 
+def empty_case(m, n):
+    """A matrix without nonzeros: m x n, alpha 2, beta -0.5."""
+    rng = np.random.default_rng(m * 10 + n)
+    return {"m": np.int64(m), "n": np.int64(n), "alpha": 2.0, "beta": -0.5,
+            "rowptr": np.zeros(m + 1, np.int32), "col": np.zeros(0, np.int32),
+            "val": np.zeros(0), "x": rng.uniform(-1, 1, n), "y0": rng.uniform(-1, 1, m),
+            "csc_val": np.zeros(0), "csc_colptr": np.zeros(n + 1, np.int32),
+            "csc_row": np.zeros(0, np.int32), "coo_row": np.zeros(0, np.int32)}
+
+
+@pytest.mark.parametrize("entry", ENTRIES)
+@pytest.mark.parametrize("shape", [(0, 5), (4, 0), (0, 0), (3, 7)])
+def test_dropin_entry_points_without_nonzeros(sblas_lib, entry, shape):
+    """No rows, no columns, or no nonzeros: y = beta * y0, no failure."""
+    from hpda_sblas_pnnl_gb300 import api
+    api.set_compat_mode(0)
+    g = empty_case(*shape)
+    for k in ([1, 2, 3] if entry in ("v1", "v2") else [2]):
+        y = g["y0"].copy()
+        r = call_entry(entry, g, y, kernel=k)
+        assert r.comp_time >= 0
+        np.testing.assert_array_equal(y, -0.5 * g["y0"])
+
+
 def compat_expected(entry, g, kernel=2, merg_opt=0):
     """The reference's ngpu = 1 result where it differs from y = aAx + by:
     nnz-split entry points touch only rows [first, last non-empty]; CSC and
