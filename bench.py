@@ -206,7 +206,8 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
                    "bytes_per_step": bytes_step, "host_threads": threads},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
-                         "kind": kind, "sample": sample},
+                         "kind": kind, "sample": sample,
+                         "gflops": round(2 * nnz * len(ts) / total / 1e9, 3)},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -318,6 +319,7 @@ def run_ours(args):
                 "frac": round(achieved / pk, 4), "traffic": None, "peak_source": pk_kind,
                 "kernel": f"tile_spmv_kernel<128,{sigma},F64> + tile_fixup_kernel",
                 "kernel_us": round(k_ms * 1e3, 2),
+                "kernel_gflops": round(2 * nnz / (k_ms * 1e-3) / 1e9, 2),
                 "bounds_note": "1 DFMA per nonzero at the measured 5.3e11 DFMA/s caps this matrix "
                                f"at {5.3e11 * bytes_step / nnz / 1e9:.0f} GB/s; one random L2 "
                                "gather per nonzero at the measured 2.8e11/s caps it at "
@@ -348,6 +350,7 @@ def run_ours(args):
         h2d = 8 * nnz + 4 * nnz + 4 * (m + 1) + 8 * n
         d2h = 8 * m
         e2e = {"value": round(bytes_step / e2e_s / 1e9, 3), "unit": "GB/s",
+               "gflops": round(2 * nnz / e2e_s / 1e9, 3),
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": round(e2e_s * 1e3, 3),
                "comm_ms": round(1e3 * statistics.mean(r.comm_time for r in rets), 3),
@@ -366,6 +369,7 @@ def run_ours(args):
             a_np = (rp_h, col_h, val_h)
             med, ts = cpu_time_spmv(a_np, x_h, m, n, 8, threads, use_ref)
             cpu = {"value": round(bytes_step / med / 1e9, 3), "unit": "GB/s", "cores": threads,
+                   "gflops": round(2 * nnz / med / 1e9, 3),
                    "kind": "reference" if use_ref else "port",
                    "sample": f"8 full SpMVs of the same matrix (median), {threads} threads"}
 
@@ -376,6 +380,7 @@ def run_ours(args):
         out = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4),
+            "gflops": round(2 * nnz * ws / (ms_step * 1e-3) / 1e9, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
             "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
@@ -447,6 +452,7 @@ def run_banded_extra(dev, stream, args, timed, threads, pk):
         err = float(np.linalg.norm(y.cpu().numpy() - ref) / nref)
         b = synth.compulsory_bytes(m, n, nnz, val_bytes=vb)
         res[name] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
+                     "gflops": round(2 * nnz / ms / 1e6, 1),
                      "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err, "nnz": nnz,
                      "sigma": sg}
         del plan
@@ -473,6 +479,7 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
     ref = O.csr_spmv(a.m, a.n, rp, c, v, x.cpu().numpy(), np.zeros(a.m), threads=threads)
     err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
     res["powerlaw_pattern"] = {"gbs": round(b / ms / 1e6, 1), "frac": round(b / ms / 1e6 / pk, 4),
+                               "gflops": round(2 * a.nnz / ms / 1e6, 1),
                                "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err,
                                "sigma": sg}
     # CSC and COO (device conversion once, then the tile kernel; conversion timed apart)
@@ -488,6 +495,7 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
         lambda: ops.coomv(row, a.col, a.val, x, y, rowptr_work=rpw), stream, 10))
     bcoo = synth.compulsory_bytes(a.m, a.n, a.nnz, fmt="coo")
     res["powerlaw_coo"] = {"gbs": round(bcoo / coo_ms / 1e6, 1),
+                           "gflops": round(2 * a.nnz / coo_ms / 1e6, 1),
                            "frac": round(bcoo / coo_ms / 1e6 / pk, 4), "us": round(coo_ms * 1e3, 1),
                            "note": "row pointer built on device each call, then tile kernel"}
     res["powerlaw_csc_to_csr_ms"] = round(conv_ms, 2)
