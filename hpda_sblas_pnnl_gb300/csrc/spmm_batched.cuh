@@ -103,10 +103,53 @@ struct Args {
 template <int K>
 constexpr int row_stride() { return K == 16 ? K + 2 : K; }
 
+// CTAs of 128 threads per SM that the registers of a shape allow (ptxas:
+// about 56-125 registers per thread for K = 1, 64 for K = 2, 80 for K = 4,
+// 126 for K = 8, 216 for K = 16).  Used only to keep the shared memory of the
+// resident CTAs within 196 KB per SM (rows_in_buffer); a stale entry costs
+// speed, never correctness.
 template <int K, int S>
+constexpr int ctas_by_registers()
+{
+    return K == 1 ? (S == 4 ? 9 : S == 8 ? 8 : S == 16 ? 6 : 4)
+                  : K == 2 ? 8 : K == 4 ? 6 : K == 8 ? 4 : 2;
+}
+
+constexpr size_t up16(size_t v) { return (v + 15) / 16 * 16; }
+
+// Shared-memory bytes of one warp (WarpSmem below) for a row capacity r.
+template <int K, int S, int VB>
+constexpr size_t warp_smem_bytes(int r)
+{
+    const size_t staged = size_t(32 * S + 32);
+    const size_t rp = up16(staged * 4 + staged * VB);
+    const size_t rbuf = up16(rp + size_t(r + 2) * 4);
+    return rbuf + size_t(r) * row_stride<K>() * 8 + size_t(32) * row_stride<K>() * 8;
+}
+
+// Rows of a unit held in the warp's row buffer: 8 S, at most 1536 / K; if
+// the CTAs that fit on an SM would then need more than 196 KB of shared
+// memory per SM (past that the driver takes the 228-KB carveout and random
+// gathers run at less than half their rate), trimmed by up to a quarter
+// until the same CTA count fits.
+template <int K, int S, int VB>
+constexpr int rows_in_buffer()
+{
+    const int r = (8 * S < 1536 / K) ? 8 * S : 1536 / K;
+    const size_t cta = 4 * warp_smem_bytes<K, S, VB>(r) + 1024;   // + the driver's 1 KB
+    int occ = (int)(size_t(228 * 1024) / cta);
+    if (occ > ctas_by_registers<K, S>()) occ = ctas_by_registers<K, S>();
+    if (occ < 1 || (size_t)occ * cta <= size_t(196 * 1024)) return r;
+    const size_t budget = size_t(196 * 1024) / occ - 1024;
+    int t = r;
+    while (t > r - r / 4 && 4 * warp_smem_bytes<K, S, VB>(t) > budget) --t;
+    return 4 * warp_smem_bytes<K, S, VB>(t) <= budget ? t : r;
+}
+
+template <int K, int S, int VB>
 struct Shape {
     static constexpr int UNIT = 32 * S;                        // nonzeros per unit
-    static constexpr int RCAP = (8 * S < 1536 / K) ? 8 * S : 1536 / K;  // rows in the buffer
+    static constexpr int RCAP = rows_in_buffer<K, S, VB>();    // rows in the buffer
     static constexpr int RPN = RCAP + 2;                       // row-pointer slice entries
 };
 
@@ -131,7 +174,7 @@ struct VT<VAL_PATTERN> {
 // shared memory of one warp
 template <int K, int S, int VK>
 struct WarpSmem {
-    using SH = Shape<K, S>;
+    using SH = Shape<K, S, VT<VK>::B>;
     static constexpr size_t COL = 0;
     // staged col and val: lane l's S entries at l*(S+1) (an odd stride for the
     // even S, so the lanes' strided reads hit different banks)
@@ -145,6 +188,9 @@ struct WarpSmem {
 template <int K, int S, int VK>
 constexpr size_t cta_smem_bytes()
 {
+    static_assert(WarpSmem<K, S, VK>::TOTAL ==
+                      warp_smem_bytes<K, S, VT<VK>::B>(Shape<K, S, VT<VK>::B>::RCAP),
+                  "warp_smem_bytes follows WarpSmem");
     return size_t(NW) * WarpSmem<K, S, VK>::TOTAL;
 }
 
@@ -208,7 +254,7 @@ __device__ __forceinline__ double finish(double v, double alpha, double beta, co
 template <int K, int S, int VK>
 __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
 {
-    using SH = Shape<K, S>;
+    using SH = Shape<K, S, VT<VK>::B>;
     using WS = WarpSmem<K, S, VK>;
     using T = typename VT<VK>::T;
     static_assert(S <= 32, "row-start mask is 32 bits");
@@ -618,8 +664,8 @@ __global__ void __launch_bounds__(CTA) batch_sddmm_kernel(const Args a)
         const int *rowptr = M->rowptr;
         const int *col = M->col;
         const int lu = u - M->unit0;
-        const int U0 = lu * Shape<K, S>::UNIT;
-        const int cntu = (int)min((long long)Shape<K, S>::UNIT, M->nnz - U0);
+        const int U0 = lu * 32 * S;
+        const int cntu = (int)min((long long)(32 * S), M->nnz - U0);
         if (lane >= cntu) continue;
         const int RA = __ldg(a.unit_row + u);
         const int RB = (lu + 1 < M->nunits) ? __ldg(a.unit_row + u + 1) : M->m - 1;

@@ -71,11 +71,47 @@ constexpr int NCW = 4;                 // compute warps per CTA
 constexpr int TC = NCW * 32;           // compute threads per CTA (one chunk each)
 constexpr int CTA_THREADS = TC + 64;   // + producer warp + epilogue warp
 
+// Shared-memory bytes of one CTA (the Layout below) for a row capacity r.
+template <int SIGMA, int VK>
+constexpr size_t layout_bytes(int r)
+{
+    const size_t tile = size_t(TC) * SIGMA;
+    const size_t rslot = size_t((r + 8 + 3) / 4 * 4);
+    const size_t col = align16(size_t(STAGES) * tile * ValTraits<VK>::BYTES);
+    const size_t rptr = align16(col + size_t(STAGES) * tile * 4);
+    const size_t meta = align16(rptr + size_t(STAGES) * rslot * 4);
+    const size_t rval = align16(meta + size_t(STAGES) * 16);
+    const size_t tailv = align16(rval + 2 * size_t(r) * 8);
+    const size_t cmeta = align16(tailv + 5 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
+    return align16(cmeta + 2 * 16) + (2 * STAGES + 4) * 8;
+}
+
+// Rows of a tile held in shared memory: TILE / 4 + 2, unless the CTAs that
+// fit on an SM (at most 4: 70 registers x 192 threads) would then need more
+// than 196 KB of shared memory per SM.  Past that the driver takes the
+// 228-KB carveout, leaves about 28 KB of L1, and random gathers of x run at
+// less than half their rate; the row capacity is then trimmed (by a quarter
+// at most) until the same CTA count fits in 196 KB.
+template <int SIGMA, int VK>
+constexpr int rows_in_smem()
+{
+    const int r = TC * SIGMA / 4 + 2;
+    const size_t cta = layout_bytes<SIGMA, VK>(r) + 1024;   // + the driver's 1 KB per CTA
+    int occ = (int)(size_t(228 * 1024) / cta);
+    if (occ > 4) occ = 4;
+    if ((size_t)occ * cta <= size_t(196 * 1024)) return r;
+    const size_t budget = size_t(196 * 1024) / occ - 1024;
+    int t = r;
+    while (t > r - r / 4 && layout_bytes<SIGMA, VK>(t) > budget) --t;
+    return layout_bytes<SIGMA, VK>(t) <= budget ? t : r;
+}
+
 template <int SIGMA, int VK>
 struct Layout {
     static constexpr int TILE = TC * SIGMA;
-    static constexpr int RCAP = TILE / 4 + 2;   // owned rows (+2) of a tile held in smem;
-                                                // denser tiles use the global-memory path
+    static constexpr int RCAP = rows_in_smem<SIGMA, VK>();  // owned rows (+2) of a tile held
+                                                            // in smem; denser tiles use the
+                                                            // global-memory path
     static constexpr int RSLOT = (RCAP + 8 + 3) / 4 * 4;  // per-stage row-pointer slot
     static constexpr int VB = ValTraits<VK>::BYTES;
     // staged tiles
@@ -95,6 +131,14 @@ struct Layout {
     static constexpr size_t BAR = align16(CMETA + 2 * 16);
     static constexpr size_t TOTAL = BAR + (2 * STAGES + 4) * 8;
 };
+
+static_assert(layout_bytes<19, VAL_F64>(Layout<19, VAL_F64>::RCAP) == Layout<19, VAL_F64>::TOTAL,
+              "layout_bytes follows Layout");
+static_assert(layout_bytes<15, VAL_F32>(Layout<15, VAL_F32>::RCAP) == Layout<15, VAL_F32>::TOTAL,
+              "layout_bytes follows Layout");
+static_assert(layout_bytes<27, VAL_PATTERN>(Layout<27, VAL_PATTERN>::RCAP) ==
+                  Layout<27, VAL_PATTERN>::TOTAL,
+              "layout_bytes follows Layout");
 
 struct TileArgs {
     int m;
