@@ -123,7 +123,7 @@ struct Mapped {
 struct ThreadResult {
     long long lines = 0;        // entry lines in the range
     long long offdiag = 0;      // stored off-diagonal entries (index < nnz)
-    long long err_line = -1;    // first bad line (1-based within the file data)
+    long long err_line = -1;    // index of the first bad entry (0-based), -1: none
     const char *err_what = nullptr;
 };
 
