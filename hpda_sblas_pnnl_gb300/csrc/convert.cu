@@ -21,6 +21,14 @@
 namespace sblas {
 namespace {
 
+// Rows prev+1 .. cur start at nonzero k (nothing for an unsorted pair).  Row
+// indices outside [0, m) never produce a write outside rowptr[0 .. m].
+__device__ __forceinline__ void rows_start_at(int prev, int cur, int m, long long k,
+                                              int *__restrict__ rowptr)
+{
+    for (int r = max(prev + 1, 0); r <= cur && r <= m; ++r) rowptr[r] = (int)k;
+}
+
 __global__ void coo_rowptr_kernel(int m, long long nnz, const int *__restrict__ row,
                                   int *__restrict__ rowptr, int *__restrict__ bad)
 {
@@ -37,7 +45,44 @@ __global__ void coo_rowptr_kernel(int m, long long nnz, const int *__restrict__ 
             continue;
         }
         // rows prev+1 .. cur start at k (row `cur` itself starts at k too)
-        for (int r = prev + 1; r <= cur && r <= m; ++r) rowptr[r] = (int)k;
+        rows_start_at(prev, cur, m, k, rowptr);
+    }
+}
+
+// The same as coo_rowptr_kernel for a 16-byte aligned row array: every
+// thread takes four consecutive nonzeros with one 16-byte load (four times
+// the bytes in flight of the one-index form, which ran at about a quarter of
+// HBM speed), the left neighbour of the first from the previous quad.
+__global__ void coo_rowptr_quad_kernel(int m, long long nnz, const int *__restrict__ row,
+                                       int *__restrict__ rowptr)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nq = nnz / 4;
+    const int4 *q4 = reinterpret_cast<const int4 *>(row);
+    auto quad = [&](const int4 v, int prev, long long k) {
+        rows_start_at(prev, min(v.x, m - 1), m, k, rowptr);
+        rows_start_at(v.x, min(v.y, m - 1), m, k + 1, rowptr);
+        rows_start_at(v.y, min(v.z, m - 1), m, k + 2, rowptr);
+        rows_start_at(v.z, min(v.w, m - 1), m, k + 3, rowptr);
+    };
+    // two quads per iteration, both loaded before either is used
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq;
+         q += 2 * stride) {
+        const long long q2 = q + stride;
+        const bool two = q2 < nq;
+        const int4 v = __ldg(q4 + q);
+        const int4 w = two ? __ldg(q4 + q2) : v;
+        const int pv = (q == 0) ? -1 : __ldg(row + 4 * q - 1);
+        const int pw = two ? __ldg(row + 4 * q2 - 1) : 0;
+        quad(v, pv, 4 * q);
+        if (two) quad(w, pw, 4 * q2);
+    }
+    // the last nnz % 4 nonzeros and the end (rows after the last nonzero)
+    for (long long k = 4 * nq + (long long)blockIdx.x * blockDim.x + threadIdx.x; k <= nnz;
+         k += stride) {
+        const int prev = (k == 0) ? -1 : __ldg(row + k - 1);
+        const int cur = (k == nnz) ? m : min(__ldg(row + k), m - 1);
+        rows_start_at(prev, cur, m, k, rowptr);
     }
 }
 
@@ -100,6 +145,9 @@ int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *row
     }
     if (nnz == 0) {
         zero_rowptr_kernel<<<grid_for((long long)m + 1, 256), 256, 0, stream>>>(m, rowptr);
+    } else if ((reinterpret_cast<uintptr_t>(coo_row) & 15) == 0) {
+        coo_rowptr_quad_kernel<<<grid_for(nnz / 4 + 1, 256), 256, 0, stream>>>(m, nnz, coo_row,
+                                                                              rowptr);
     } else {
         coo_rowptr_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(m, nnz, coo_row, rowptr,
                                                                     nullptr);

@@ -327,3 +327,26 @@ def test_fp32_values_with_subnormals_and_huge_entries(sblas_lib, cuda):
     assert rel_l2(yy / scale, ref / scale) <= 1e-12
     small = np.abs(ref) < 1e30
     assert rel_l2(yy[small], ref[small]) <= 1e-12
+
+@pytest.mark.parametrize("nnz", [1, 2, 3, 4, 5, 7, 8, 1000, 1001, 1_000_003])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_coo_row_pointer_builder(sblas_lib, cuda, nnz, offset):
+    """Row pointer of row-sorted COO built on the device (the step before
+    the COO SpMV; the reference's coo2csrGPU), against numpy: rows empty at
+    the start, middle and end; a 16-byte aligned row array (the four-index
+    kernel) and one misaligned by 4 bytes (the one-index kernel)."""
+    import ctypes as C
+    rng = np.random.default_rng(nnz + offset)
+    m = max(8, nnz // 3)
+    rows = np.sort(rng.integers(2, m - 2, nnz)).astype(np.int32)
+    buf = torch.zeros(nnz + 1, dtype=torch.int32, device=cuda)
+    buf[offset:offset + nnz] = torch.from_numpy(rows).to(cuda)
+    row = buf[offset:offset + nnz]
+    rp = torch.full((m + 1,), -7, dtype=torch.int32, device=cuda)
+    stream = C.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
+    rc = sblas_lib.sblas_coo_rows_to_rowptr(m, nnz, C.c_void_p(row.data_ptr()),
+                                            C.c_void_p(rp.data_ptr()), stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    want = np.searchsorted(rows, np.arange(m + 1), side="left").astype(np.int32)
+    np.testing.assert_array_equal(rp.cpu().numpy(), want)
