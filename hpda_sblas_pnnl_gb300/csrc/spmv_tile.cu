@@ -633,6 +633,16 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
 // One streaming pass over the row pointer: the row r with
 // rowptr[r] <= k*TILE < rowptr[r+1] is the only one whose count is r, so
 // every non-empty row writes its own value into the entries it covers.
+__device__ __forceinline__ void own_tiles(int r, long long b, long long e, int ntiles,
+                                          long long tile, int *__restrict__ part)
+{
+    if (e <= b) return;
+    long long k = (b + tile - 1) / tile;      // first k with k*tile >= b
+    const long long k1 = (e - 1) / tile;      // last k with k*tile <= e-1
+    if (k < 1) k = 1;
+    for (; k <= k1 && k < ntiles; ++k) part[k] = r;
+}
+
 __global__ void tile_partition_kernel(int m, long long nnz, int ntiles, long long tile,
                                       const int *__restrict__ rowptr, int *__restrict__ part)
 {
@@ -643,14 +653,43 @@ __global__ void tile_partition_kernel(int m, long long nnz, int ntiles, long lon
         part[0] = 0;
         part[ntiles] = m;
     }
-    for (int r = g; r < m; r += stride) {
-        const long long b = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-        if (e <= b) continue;
-        long long k = (b + tile - 1) / tile;      // first k with k*tile >= b
-        const long long k1 = (e - 1) / tile;      // last k with k*tile <= e-1
-        if (k < 1) k = 1;
-        for (; k <= k1 && k < ntiles; ++k) part[k] = r;
+    for (int r = g; r < m; r += stride)
+        own_tiles(r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, tile, part);
+}
+
+// The same pass for a 16-byte aligned row pointer: four rows per thread from
+// one 16-byte load (plus the next entry), two such loads in flight; one row
+// per thread kept too few bytes in flight to stream the row pointer.
+__global__ void tile_partition_quad_kernel(int m, int ntiles, long long tile,
+                                           const int *__restrict__ rowptr,
+                                           int *__restrict__ part)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g == 0) {
+        part[0] = 0;
+        part[ntiles] = m;
     }
+    const long long nq = m / 4;
+    const int4 *q4 = reinterpret_cast<const int4 *>(rowptr);
+    auto quad = [&](const int4 v, int next, long long r0) {
+        own_tiles((int)r0, v.x, v.y, ntiles, tile, part);
+        own_tiles((int)r0 + 1, v.y, v.z, ntiles, tile, part);
+        own_tiles((int)r0 + 2, v.z, v.w, ntiles, tile, part);
+        own_tiles((int)r0 + 3, v.w, next, ntiles, tile, part);
+    };
+    for (long long q = g; q < nq; q += 2 * stride) {
+        const long long q2 = q + stride;
+        const bool two = q2 < nq;
+        const int4 v = __ldg(q4 + q);
+        const int ve = __ldg(rowptr + 4 * q + 4);
+        const int4 w = two ? __ldg(q4 + q2) : v;
+        const int we = two ? __ldg(rowptr + 4 * q2 + 4) : 0;
+        quad(v, ve, 4 * q);
+        if (two) quad(w, we, 4 * q2);
+    }
+    for (long long r = 4 * nq + g; r < m; r += stride)
+        own_tiles((int)r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, tile, part);
 }
 
 // Adds the carries of the tiles a row spans to the row, in tile order.
@@ -807,8 +846,16 @@ int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void
     const int ntiles = (int)ntiles_ll;
     int *part = static_cast<int *>(work);
     const int threads = 256;
-    const int blocks = min((m + threads - 1) / threads, 8 * device_num_sms());
-    tile_partition_kernel<<<blocks, threads, 0, stream>>>(m, nnz, ntiles, tile, rowptr, part);
+    if ((reinterpret_cast<uintptr_t>(rowptr) & 15) == 0) {
+        const int quads = m / 4 + 1;
+        const int blocks = min((quads + threads - 1) / threads, 8 * device_num_sms());
+        tile_partition_quad_kernel<<<blocks, threads, 0, stream>>>(m, ntiles, tile, rowptr,
+                                                                   part);
+    } else {
+        const int blocks = min((m + threads - 1) / threads, 8 * device_num_sms());
+        tile_partition_kernel<<<blocks, threads, 0, stream>>>(m, nnz, ntiles, tile, rowptr,
+                                                              part);
+    }
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }
