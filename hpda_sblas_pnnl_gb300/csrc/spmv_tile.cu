@@ -633,14 +633,20 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
 // One streaming pass over the row pointer: the row r with
 // rowptr[r] <= k*TILE < rowptr[r+1] is the only one whose count is r, so
 // every non-empty row writes its own value into the entries it covers.
-__device__ __forceinline__ void own_tiles(int r, long long b, long long e, int ntiles,
-                                          long long tile, int *__restrict__ part)
+// Tiles k (1 <= k < ntiles) whose first nonzero k*tile lies in row r =
+// [b, e) get part[k] = r.  One 32-bit division per row (64-bit divisions,
+// two per row, made this pass issue-bound): most rows hold no tile start,
+// and the second division only runs for rows that do.
+__device__ __forceinline__ void own_tiles(int r, int b, int e, int ntiles, unsigned tile,
+                                          int *__restrict__ part)
 {
     if (e <= b) return;
-    long long k = (b + tile - 1) / tile;      // first k with k*tile >= b
-    const long long k1 = (e - 1) / tile;      // last k with k*tile <= e-1
-    if (k < 1) k = 1;
-    for (; k <= k1 && k < ntiles; ++k) part[k] = r;
+    const unsigned k1 = (unsigned)(e - 1) / tile;             // last k with k*tile <= e-1
+    const unsigned long long top = (unsigned long long)k1 * tile;
+    if (top < (unsigned long long)b) return;                   // no tile starts in the row
+    unsigned k = k1 - (unsigned)((top - (unsigned long long)b) / tile);   // first k*tile >= b
+    if (k < 1u) k = 1u;
+    for (; k <= k1 && k < (unsigned)ntiles; ++k) part[k] = r;
 }
 
 __global__ void tile_partition_kernel(int m, long long nnz, int ntiles, long long tile,
@@ -654,7 +660,7 @@ __global__ void tile_partition_kernel(int m, long long nnz, int ntiles, long lon
         part[ntiles] = m;
     }
     for (int r = g; r < m; r += stride)
-        own_tiles(r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, tile, part);
+        own_tiles(r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, (unsigned)tile, part);
 }
 
 // The same pass for a 16-byte aligned row pointer: four rows per thread from
@@ -672,11 +678,12 @@ __global__ void tile_partition_quad_kernel(int m, int ntiles, long long tile,
     }
     const long long nq = m / 4;
     const int4 *q4 = reinterpret_cast<const int4 *>(rowptr);
+    const unsigned t32 = (unsigned)tile;
     auto quad = [&](const int4 v, int next, long long r0) {
-        own_tiles((int)r0, v.x, v.y, ntiles, tile, part);
-        own_tiles((int)r0 + 1, v.y, v.z, ntiles, tile, part);
-        own_tiles((int)r0 + 2, v.z, v.w, ntiles, tile, part);
-        own_tiles((int)r0 + 3, v.w, next, ntiles, tile, part);
+        own_tiles((int)r0, v.x, v.y, ntiles, t32, part);
+        own_tiles((int)r0 + 1, v.y, v.z, ntiles, t32, part);
+        own_tiles((int)r0 + 2, v.z, v.w, ntiles, t32, part);
+        own_tiles((int)r0 + 3, v.w, next, ntiles, t32, part);
     };
     for (long long q = g; q < nq; q += 2 * stride) {
         const long long q2 = q + stride;
@@ -689,7 +696,7 @@ __global__ void tile_partition_quad_kernel(int m, int ntiles, long long tile,
         if (two) quad(w, we, 4 * q2);
     }
     for (long long r = 4 * nq + g; r < m; r += stride)
-        own_tiles((int)r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, tile, part);
+        own_tiles((int)r, __ldg(rowptr + r), __ldg(rowptr + r + 1), ntiles, t32, part);
 }
 
 // Adds the carries of the tiles a row spans to the row, in tile order.
