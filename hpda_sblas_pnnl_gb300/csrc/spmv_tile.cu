@@ -80,11 +80,10 @@ constexpr size_t layout_bytes(int r)
     const size_t col = align16(size_t(STAGES) * tile * ValTraits<VK>::BYTES);
     const size_t rptr = align16(col + size_t(STAGES) * tile * 4);
     const size_t meta = align16(rptr + size_t(STAGES) * rslot * 4);
-    const size_t chunk = align16(meta + size_t(STAGES) * 16);
-    const size_t rval = align16(chunk + size_t(STAGES) * TC * 16);
+    const size_t rval = align16(meta + size_t(STAGES) * 16);
     const size_t tailv = align16(rval + 2 * size_t(r) * 8);
     const size_t cmeta = align16(tailv + 5 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
-    return align16(cmeta + 2 * 16) + (3 * STAGES + 4) * 8;
+    return align16(cmeta + 2 * 16) + (2 * STAGES + 4) * 8;
 }
 
 // Rows of a tile held in shared memory: TILE / 4 + 2, unless the CTAs that
@@ -120,19 +119,17 @@ struct Layout {
     static constexpr size_t COL = align16(VAL + size_t(STAGES) * TILE * VB);
     static constexpr size_t RPTR = align16(COL + size_t(STAGES) * TILE * 4);
     static constexpr size_t META = align16(RPTR + size_t(STAGES) * RSLOT * 4);
-    // per-chunk row metadata of a staged tile (int4 per chunk, by the producer)
-    static constexpr size_t CHUNK = align16(META + size_t(STAGES) * 16);
     // carry buffers, double-buffered by tile parity
-    static constexpr size_t RVAL = align16(CHUNK + size_t(STAGES) * TC * 16);
+    static constexpr size_t RVAL = align16(META + size_t(STAGES) * 16);
     static constexpr size_t TAILV = align16(RVAL + 2 * size_t(RCAP) * 8);
     static constexpr size_t HEADV = TAILV + 2 * size_t(TC) * 8;
     static constexpr size_t CIN = HEADV + 2 * size_t(TC) * 8;
     static constexpr size_t TAILK = CIN + size_t(TC) * 8;
     static constexpr size_t HEADK = TAILK + 2 * size_t(TC) * 4;
     static constexpr size_t CMETA = align16(HEADK + 2 * size_t(TC) * 4);
-    // mbarriers: full[STAGES], empty[STAGES], cfull[2], cempty[2], mready[STAGES]
+    // mbarriers: full[STAGES], empty[STAGES], cfull[2], cempty[2]
     static constexpr size_t BAR = align16(CMETA + 2 * 16);
-    static constexpr size_t TOTAL = BAR + (3 * STAGES + 4) * 8;
+    static constexpr size_t TOTAL = BAR + (2 * STAGES + 4) * 8;
 };
 
 static_assert(layout_bytes<19, VAL_F64>(Layout<19, VAL_F64>::RCAP) == Layout<19, VAL_F64>::TOTAL,
@@ -181,7 +178,6 @@ struct Smem {
     __device__ int *col(int s) const { return reinterpret_cast<int *>(base + L::COL) + size_t(s) * L::TILE; }
     __device__ int *rptr(int s) const { return reinterpret_cast<int *>(base + L::RPTR) + size_t(s) * L::RSLOT; }
     __device__ int *meta(int s) const { return reinterpret_cast<int *>(base + L::META) + 4 * s; }
-    __device__ int4 *chunk(int s) const { return reinterpret_cast<int4 *>(base + L::CHUNK) + s * TC; }
     __device__ double *rval(int p) const { return reinterpret_cast<double *>(base + L::RVAL) + size_t(p) * L::RCAP; }
     __device__ double *tailv(int p) const { return reinterpret_cast<double *>(base + L::TAILV) + p * TC; }
     __device__ double *headv(int p) const { return reinterpret_cast<double *>(base + L::HEADV) + p * TC; }
@@ -194,7 +190,6 @@ struct Smem {
     __device__ uint64_t *empty(int s) const { return bar() + STAGES + s; }
     __device__ uint64_t *cfull(int p) const { return bar() + 2 * STAGES + p; }
     __device__ uint64_t *cempty(int p) const { return bar() + 2 * STAGES + 2 + p; }
-    __device__ uint64_t *mready(int s) const { return bar() + 2 * STAGES + 4 + s; }
 };
 
 // Stages tile `tile` into stage `s` (the producer warp, all lanes): owned-row
@@ -288,10 +283,7 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
     for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
         const int s = i % STAGES;
         const int p = i & 1;
-        bool ok = ptx::mbar_wait_bounded(sm.mready(s), (uint32_t)((i / STAGES) & 1),
-                                         WAIT_LIMIT_NS);
-        ok = ok && ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1),
-                                          WAIT_LIMIT_NS);
+        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), WAIT_LIMIT_NS);
         if (i >= 2)
             ok = ok && ptx::mbar_wait_bounded(sm.cempty(p), (uint32_t)(((i - 2) / 2) & 1),
                                               WAIT_LIMIT_NS);
@@ -320,12 +312,10 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
         bool sb = false;           // the first row began before the chunk
         unsigned mask = 0;         // bit j: nonzero j of the chunk starts a new row
         bool slow = !fits;         // empty rows inside the chunk, or rows not in smem
-        // the producer's row metadata of this chunk (read before the gathers
-        // queue up in the load pipeline)
-        const int4 cmv = fits ? sm.chunk(s)[t] : make_int4(R0, R0, 0, 0);
         if (cnt > 0) {
             // issue every gather of the chunk first (one L2 round trip per
-            // chunk instead of one per nonzero)
+            // chunk instead of one per nonzero); the row search below runs
+            // while they are in flight
             if (cnt == SIGMA) {
 #pragma unroll
                 for (int j = 0; j < SIGMA; ++j)
@@ -335,32 +325,25 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
                 for (int j = 0; j < SIGMA; ++j)
                     xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + (j < cnt ? j : 0)], pol_x);
             }
-            if (fits) {
-                const unsigned bits = (unsigned)cmv.z;
-                r0 = cmv.x;
-                rl = cmv.y;
-                sb = (bits >> 31) != 0u;
-                slow = ((bits >> 30) & 1u) != 0u;
-                mask = bits & 0x3FFFFFFFu;
-            } else {
-                // rows not in shared memory: search the global row pointer;
-                // last row r in [R0, R1] with rowptr[r] <= s0
-                int lo = R0, hi = min(R1, a.m - 1);
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (rp(mid) <= s0) lo = mid; else hi = mid - 1;
-                }
-                r0 = lo;
-                sb = rp(r0) < s0;
-                int rr = r0, nx = rp(r0 + 1);
-                const int send = s0 + cnt;
-                while (nx < send) {
-                    mask |= 1u << (nx - s0);
-                    ++rr;
-                    nx = rp(rr + 1);
-                }
-                rl = rr;
+            // last row r in [R0, R1] with rowptr[r] <= s0
+            int lo = R0, hi = min(R1, a.m - 1);
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rp(mid) <= s0) lo = mid; else hi = mid - 1;
             }
+            r0 = lo;
+            sb = rp(r0) < s0;
+            // row starts strictly inside the chunk -> boundary bits
+            int rr = r0, nx = rp(r0 + 1);
+            const int send = s0 + cnt;
+            while (nx < send) {
+                mask |= 1u << (nx - s0);
+                const int n2 = rp(rr + 2);
+                slow |= (n2 == nx);   // an empty row follows: general path
+                ++rr;
+                nx = n2;
+            }
+            rl = rr;
         }
         const bool warp_slow = __any_sync(0xffffffffu, slow);
         double sum = 0.0;
@@ -444,88 +427,6 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
     }
 }
 
-// Row metadata of every chunk of a staged tile whose row-pointer slice is in
-// shared memory (producer warp, 4 chunks per lane, searches interleaved):
-// {first row, last row, row-start bits, 0}.  Bit j (1 <= j < SIGMA) of the
-// bits: nonzero j of the chunk starts a row; bit 31: the first row began
-// before the chunk; bit 30: an empty row starts inside the chunk (the compute
-// warps then take their general path).  Computed here, off the compute
-// warps' critical path, where the row search used to wait behind the gathers.
-template <int SIGMA, int VK>
-__device__ __forceinline__ void chunk_meta(const TileArgs &a, const Smem<SIGMA, VK> &sm,
-                                           int tile, int s, int lane)
-{
-    using L = Layout<SIGMA, VK>;
-    static_assert(SIGMA <= 30, "row-start bits share the word with two flags");
-    constexpr int PER = TC / 32;
-    const int *meta = sm.meta(s);
-    if (meta[3] == 0) return;                  // slice not in shared memory
-    const int R0 = meta[0], R1 = meta[1], rbase = meta[2];
-    const int *rs = sm.rptr(s);
-    const long long tb = (long long)tile * L::TILE;
-    const int cnt_tile = (int)((a.nnz - tb < L::TILE) ? (a.nnz - tb) : L::TILE);
-    const int hi0 = min(R1, a.m - 1);
-    int lo[PER], hi[PER], s0[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        s0[q] = (int)(tb + (long long)(q * 32 + lane) * SIGMA);
-        lo[q] = R0;
-        hi[q] = hi0;
-    }
-    // last row r in [R0, R1] with rowptr[r] <= s0, the PER searches in step
-    for (bool more = true; more;) {
-        more = false;
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            if (lo[q] < hi[q]) {
-                const int mid = (lo[q] + hi[q] + 1) >> 1;
-                if (rs[mid - rbase] <= s0[q]) lo[q] = mid; else hi[q] = mid - 1;
-                more |= lo[q] < hi[q];
-            }
-        }
-    }
-    int4 *out = sm.chunk(s);
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int c = q * 32 + lane;
-        const int cnt = max(0, min(SIGMA, cnt_tile - c * SIGMA));
-        int r0 = R0, rr = R0;
-        unsigned bits = 0;
-        if (cnt > 0) {
-            r0 = lo[q];
-            if (rs[r0 - rbase] < s0[q]) bits |= 1u << 31;
-            rr = r0;
-            int nx = rs[r0 + 1 - rbase];
-            const int send = s0[q] + cnt;
-            while (nx < send) {
-                bits |= 1u << (nx - s0[q]);
-                const int n2 = rs[rr + 2 - rbase];
-                if (n2 == nx) bits |= 1u << 30;
-                ++rr;
-                nx = n2;
-            }
-        }
-        out[c] = make_int4(r0, rr, (int)bits, 0);
-    }
-}
-
-// Waits for the copies of stage s (the phase-th use of the stage), computes
-// its chunk metadata and releases the stage to the compute warps.
-template <int SIGMA, int VK>
-__device__ __forceinline__ bool publish_stage(const TileArgs &a, const Smem<SIGMA, VK> &sm,
-                                              int tile, int s, uint32_t phase, int lane)
-{
-    const bool ok = ptx::mbar_wait_bounded(sm.full(s), phase, WAIT_LIMIT_NS);
-    if (!__all_sync(0xffffffffu, ok)) {
-        if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
-        return false;
-    }
-    chunk_meta<SIGMA, VK>(a, sm, tile, s, lane);
-    __syncwarp();
-    if (lane == 0) ptx::mbar_arrive(sm.mready(s));
-    return true;
-}
-
 // Producer warp: stages the CTA's tiles into the STAGES-deep ring, each as
 // soon as the compute warps release its stage; the tile's partition entries
 // are loaded before that wait, so their latency hides behind it.
@@ -544,12 +445,7 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
             ++issued[s];
         }
     }
-    bool alive = true;
-    for (int s = 0; s < STAGES && alive; ++s) {
-        const int t = blockIdx.x + s * (int)gridDim.x;
-        if (t < a.ntiles) alive = publish_stage<SIGMA, VK>(a, sm, t, s, 0u, lane);
-    }
-    for (int i = 0, nt = blockIdx.x + STAGES * (int)gridDim.x; alive && nt < a.ntiles;
+    for (int i = 0, nt = blockIdx.x + STAGES * (int)gridDim.x; nt < a.ntiles;
          ++i, nt += gridDim.x) {
         const int s = i % STAGES;
         const int R0 = __ldg(a.row_part + nt);
@@ -563,7 +459,6 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
         ptx::fence_proxy_async_smem();
         produce_tile<SIGMA, VK>(a, sm, nt, s, R0, R1, lane, pol_stream);
         ++issued[s];
-        alive = publish_stage<SIGMA, VK>(a, sm, nt, s, (uint32_t)((issued[s] - 1) & 1), lane);
     }
     // the CTA may exit only when no copy into its shared memory is in flight
     if (lane == 0) {
@@ -718,9 +613,6 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
         for (int p = 0; p < 2; ++p) {
             ptx::mbar_init(sm.cfull(p), NCW);
             ptx::mbar_init(sm.cempty(p), 1);
-        }
-        for (int s = 0; s < STAGES; ++s) {
-            ptx::mbar_init(sm.mready(s), 1);
         }
         ptx::fence_mbar_init();
     }
