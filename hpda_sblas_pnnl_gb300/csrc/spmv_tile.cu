@@ -313,19 +313,9 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
         unsigned mask = 0;         // bit j: nonzero j of the chunk starts a new row
         bool slow = !fits;         // empty rows inside the chunk, or rows not in smem
         if (cnt > 0) {
-            // issue every gather of the chunk first (one L2 round trip per
-            // chunk instead of one per nonzero); the row search below runs
-            // while they are in flight
-            if (cnt == SIGMA) {
-#pragma unroll
-                for (int j = 0; j < SIGMA; ++j)
-                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + j], pol_x);
-            } else {
-#pragma unroll
-                for (int j = 0; j < SIGMA; ++j)
-                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + (j < cnt ? j : 0)], pol_x);
-            }
-            // last row r in [R0, R1] with rowptr[r] <= s0
+            // the chunk's rows first: the dependent shared-memory reads of
+            // the search would otherwise wait behind the gathers in the
+            // load pipeline.  Last row r in [R0, R1] with rowptr[r] <= s0
             int lo = R0, hi = min(R1, a.m - 1);
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
@@ -344,6 +334,17 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
                 nx = n2;
             }
             rl = rr;
+            // then every gather of the chunk (one L2 round trip per chunk
+            // instead of one per nonzero)
+            if (cnt == SIGMA) {
+#pragma unroll
+                for (int j = 0; j < SIGMA; ++j)
+                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + j], pol_x);
+            } else {
+#pragma unroll
+                for (int j = 0; j < SIGMA; ++j)
+                    xv[j] = ptx::ldg_x_issue(a.x + cst[c0 + (j < cnt ? j : 0)], pol_x);
+            }
         }
         const bool warp_slow = __any_sync(0xffffffffu, slow);
         double sum = 0.0;
