@@ -29,7 +29,7 @@
 namespace sblas {
 namespace {
 
-constexpr size_t kNoallocScratchBytes = size_t(4) << 20;  // 4 MiB
+constexpr size_t kNoallocScratchBytes = size_t(7) << 20;  // 7 MiB: ~0.86 G nonzeros at sigma 11
 constexpr int kMaxDev = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];

@@ -804,9 +804,12 @@ size_t tile_workspace_bytes(long long nnz, int sigma)
 
 int default_sigma_for(int m, long long nnz)
 {
+    // measured best on both benchmark matrices (power-law 312 us, banded
+    // 802 us; sigma 15: 317 / 830, 19: 327 / 935); the tuner measures the
+    // caller's own matrix
     (void)m;
     (void)nnz;
-    return 19;
+    return 11;
 }
 
 int csr5_sigma_for(int m, long long nnz)

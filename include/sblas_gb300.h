@@ -115,8 +115,8 @@ SBLAS_API int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, dou
  * device memory at start-up and forbid allocation afterwards.  This entry
  * point has no counterpart in the reference.
  * Scratch: a fixed file-scope device array of sblas_noalloc_scratch_bytes()
- * bytes (4 MiB, held by every GPU that loads the library until exit); larger
- * matrices (about 0.8 G nonzeros and up) fail with SBLAS_ERR_ARG.  The
+ * bytes (7 MiB, held by every GPU that loads the library until exit); larger
+ * matrices (about 0.86 G nonzeros and up) fail with SBLAS_ERR_ARG.  The
  * array is shared by every call: calls that overlap on the GPU race.  The
  * first call on a device resolves the array's address and creates the
  * library's per-device context (no device memory): make it before any
