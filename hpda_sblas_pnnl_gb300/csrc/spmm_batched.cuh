@@ -135,12 +135,13 @@ constexpr size_t warp_smem_bytes(int r)
 template <int K, int S, int VB>
 constexpr int rows_in_buffer()
 {
+    constexpr size_t kLimit = size_t(195) * 1024;   // 196 KB less a 1-KB margin
     const int r = (8 * S < 1536 / K) ? 8 * S : 1536 / K;
     const size_t cta = 4 * warp_smem_bytes<K, S, VB>(r) + 1024;   // + the driver's 1 KB
     int occ = (int)(size_t(228 * 1024) / cta);
     if (occ > ctas_by_registers<K, S>()) occ = ctas_by_registers<K, S>();
-    if (occ < 1 || (size_t)occ * cta <= size_t(196 * 1024)) return r;
-    const size_t budget = size_t(196 * 1024) / occ - 1024;
+    if (occ < 1 || (size_t)occ * cta <= kLimit) return r;
+    const size_t budget = kLimit / occ - 1024;
     int t = r;
     while (t > r - r / 4 && 4 * warp_smem_bytes<K, S, VB>(t) > budget) --t;
     return 4 * warp_smem_bytes<K, S, VB>(t) <= budget ? t : r;

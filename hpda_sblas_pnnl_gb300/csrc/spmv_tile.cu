@@ -14,13 +14,14 @@
 //  * warp-specialised persistent CTA: 4 compute warps (one chunk of SIGMA
 //    nonzeros per lane), a producer warp staging tiles into a STAGES-deep
 //    shared-memory ring with 1-D bulk copies (cp.async.bulk, L2 evict-first),
-//    and an epilogue warp merging the chunk carries one tile behind;
+//    and two epilogue warps (one per tile parity) merging the chunk carries
+//    one tile behind;
 //    mbarrier hand-offs, every wait bounded, no CTA-wide barrier in the loop;
 //  * every lane runs exactly SIGMA fused multiply-adds with all 32 lanes
 //    active; a row ending inside the chunk only costs integer work and a
 //    shared-memory store (the running sum restarts with a select);
 //  * the per-lane partial of the row crossing a chunk boundary ("tail") is
-//    combined by the epilogue warp: runs of equal rows reduced lane-
+//    combined by an epilogue warp: runs of equal rows reduced lane-
 //    sequentially (NCW adds per lane, work-efficient) and a 5-step segmented
 //    shuffle scan joining runs crossing lanes; the lane that holds the end of
 //    the row adds the result to its partial ("head") once;
@@ -69,7 +70,8 @@ struct ValTraits<VAL_PATTERN> {
 
 constexpr int NCW = 4;                 // compute warps per CTA
 constexpr int TC = NCW * 32;           // compute threads per CTA (one chunk each)
-constexpr int CTA_THREADS = TC + 64;   // + producer warp + epilogue warp
+constexpr int NEW = 2;                 // epilogue warps: one per tile parity
+constexpr int CTA_THREADS = TC + 32 + 32 * NEW;   // + producer warp + epilogue warps
 
 // Shared-memory bytes of one CTA (the Layout below) for a row capacity r.
 template <int SIGMA, int VK>
@@ -82,12 +84,12 @@ constexpr size_t layout_bytes(int r)
     const size_t meta = align16(rptr + size_t(STAGES) * rslot * 4);
     const size_t rval = align16(meta + size_t(STAGES) * 16);
     const size_t tailv = align16(rval + 2 * size_t(r) * 8);
-    const size_t cmeta = align16(tailv + 5 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
+    const size_t cmeta = align16(tailv + 6 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
     return align16(cmeta + 2 * 16) + (2 * STAGES + 4) * 8;
 }
 
 // Rows of a tile held in shared memory: TILE / 4 + 2, unless the CTAs that
-// fit on an SM (at most 4: 70 registers x 192 threads) would then need more
+// fit on an SM (at most 4: ~56-70 registers x 224 threads) would then need more
 // than 196 KB of shared memory per SM.  Past that the driver takes the
 // 228-KB carveout, leaves about 28 KB of L1, and random gathers of x run at
 // less than half their rate; the row capacity is then trimmed (by a quarter
@@ -95,12 +97,13 @@ constexpr size_t layout_bytes(int r)
 template <int SIGMA, int VK>
 constexpr int rows_in_smem()
 {
+    constexpr size_t kLimit = size_t(195) * 1024;   // 196 KB less a 1-KB margin
     const int r = TC * SIGMA / 4 + 2;
     const size_t cta = layout_bytes<SIGMA, VK>(r) + 1024;   // + the driver's 1 KB per CTA
     int occ = (int)(size_t(228 * 1024) / cta);
     if (occ > 4) occ = 4;
-    if ((size_t)occ * cta <= size_t(196 * 1024)) return r;
-    const size_t budget = size_t(196 * 1024) / occ - 1024;
+    if ((size_t)occ * cta <= kLimit) return r;
+    const size_t budget = kLimit / occ - 1024;
     int t = r;
     while (t > r - r / 4 && layout_bytes<SIGMA, VK>(t) > budget) --t;
     return layout_bytes<SIGMA, VK>(t) <= budget ? t : r;
@@ -124,7 +127,7 @@ struct Layout {
     static constexpr size_t TAILV = align16(RVAL + 2 * size_t(RCAP) * 8);
     static constexpr size_t HEADV = TAILV + 2 * size_t(TC) * 8;
     static constexpr size_t CIN = HEADV + 2 * size_t(TC) * 8;
-    static constexpr size_t TAILK = CIN + size_t(TC) * 8;
+    static constexpr size_t TAILK = CIN + 2 * size_t(TC) * 8;
     static constexpr size_t HEADK = TAILK + 2 * size_t(TC) * 4;
     static constexpr size_t CMETA = align16(HEADK + 2 * size_t(TC) * 4);
     // mbarriers: full[STAGES], empty[STAGES], cfull[2], cempty[2]
@@ -181,7 +184,7 @@ struct Smem {
     __device__ double *rval(int p) const { return reinterpret_cast<double *>(base + L::RVAL) + size_t(p) * L::RCAP; }
     __device__ double *tailv(int p) const { return reinterpret_cast<double *>(base + L::TAILV) + p * TC; }
     __device__ double *headv(int p) const { return reinterpret_cast<double *>(base + L::HEADV) + p * TC; }
-    __device__ double *cin() const { return reinterpret_cast<double *>(base + L::CIN); }
+    __device__ double *cin(int p) const { return reinterpret_cast<double *>(base + L::CIN) + p * TC; }
     __device__ int *tailk(int p) const { return reinterpret_cast<int *>(base + L::TAILK) + p * TC; }
     __device__ int *headk(int p) const { return reinterpret_cast<int *>(base + L::HEADK) + p * TC; }
     __device__ int *cmeta(int p) const { return reinterpret_cast<int *>(base + L::CMETA) + 4 * p; }
@@ -479,12 +482,15 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
 //   epilogue: alpha/beta once per row, coalesced stores of y.
 template <int SIGMA, int VK, int AB>
 __device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
-                                              int lane)
+                                              int par, int lane)
 {
     constexpr int PER = NCW;  // tails reduced per lane
     const double alpha = a.alpha, beta = a.beta;
-    double *cin = sm.cin();
-    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+    double *cin = sm.cin(par);
+    // this warp takes the tiles of parity `par` (the CTA's tiles i = par,
+    // par + 2, ...): the carry buffers are double-buffered by that parity
+    for (int i = par, tile = blockIdx.x + par * (int)gridDim.x; tile < a.ntiles;
+         i += 2, tile += 2 * (int)gridDim.x) {
         const int p = i & 1;
         const bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1),
                                                WAIT_LIMIT_NS);
@@ -618,12 +624,12 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
         ptx::fence_mbar_init();
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
-    for (int i = tid; i < TC; i += CTA_THREADS) sm.cin()[i] = 0.0;
+    for (int i = tid; i < 2 * TC; i += CTA_THREADS) sm.cin(0)[i] = 0.0;
     __syncthreads();
     if (warp == NCW)
         producer_warp<SIGMA, VK>(a, sm, lane, ptx::policy_evict_first());
-    else if (warp == NCW + 1)
-        epilogue_warp<SIGMA, VK, AB>(a, sm, lane);
+    else if (warp > NCW)
+        epilogue_warp<SIGMA, VK, AB>(a, sm, warp - NCW - 1, lane);
     else
         compute_warp<SIGMA, VK, AB>(a, sm, warp, lane, ptx::policy_evict_last());
 }
