@@ -17,6 +17,10 @@
 //    and two epilogue warps (one per tile parity) merging the chunk carries
 //    one tile behind;
 //    mbarrier hand-offs, every wait bounded, no CTA-wide barrier in the loop;
+//  * each lane finds its chunk's rows in the staged row-pointer slice
+//    (binary search + row-start bits) before it issues the chunk's gathers:
+//    issued after them, the search's dependent shared-memory reads waited
+//    behind the gathers in the load pipeline;
 //  * every lane runs exactly SIGMA fused multiply-adds with all 32 lanes
 //    active; a row ending inside the chunk only costs integer work and a
 //    shared-memory store (the running sum restarts with a select);
@@ -273,7 +277,7 @@ __device__ __forceinline__ double widen_f32(float v)
 // nonzeros per lane.  Row sums completed inside the chunk go to the carry
 // buffer of the tile's parity; the chunk's head (first segment of a row
 // begun earlier) and tail (partial of the row crossing the chunk end) are
-// published for the epilogue warp.  No CTA-wide barrier.
+// published for the epilogue warp of the tile's parity.  No CTA-wide barrier.
 template <int SIGMA, int VK, int AB>
 __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
                                              int cw, int lane, uint64_t pol_x)
