@@ -350,3 +350,32 @@ def test_coo_row_pointer_builder(sblas_lib, cuda, nnz, offset):
     torch.cuda.synchronize()
     want = np.searchsorted(rows, np.arange(m + 1), side="left").astype(np.int32)
     np.testing.assert_array_equal(rp.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("kernel", [1, 2, 3])
+def test_misaligned_device_arrays(sblas_lib, cuda, kernel):
+    """Row pointer, columns and values as views 4 / 8 bytes past a 16-byte
+    boundary: the tile kernel stages them with plain loads instead of bulk
+    copies and partitions with the one-row-per-thread pass; results as for
+    aligned arrays.  Power-law matrix of 200k rows, every tile shape."""
+    from hpda_sblas_pnnl_gb300 import ops, synth
+    a, x = synth.powerlaw(m=200_000, mean_deg=12.0, seed=77, values="normal")
+    rp, col, val = a.numpy()
+
+    def shifted(arr, dt):
+        buf = torch.zeros(arr.size + 1, dtype=dt, device=cuda)
+        buf[1:] = torch.from_numpy(np.ascontiguousarray(arr)).to(cuda)
+        return buf[1:]
+
+    d_rp, d_col, d_val = shifted(rp, torch.int32), shifted(col, torch.int32), shifted(val,
+                                                                                   torch.float64)
+    assert d_rp.data_ptr() % 16 != 0 and d_val.data_ptr() % 16 != 0
+    xd = x.to(cuda)
+    y0 = torch.randn(a.m, dtype=torch.float64, device=cuda)
+    ref = O.csr_spmv(a.m, a.n, rp, col, val, x.numpy(), y0.cpu().numpy(), 1.5, -0.5)
+    sig = sigmas() if kernel != 1 else [0]
+    for s in sig:
+        y = y0.clone()
+        ops.csrmv(d_rp, d_col, d_val, xd, y, 1.5, -0.5, n=a.n, kernel=kernel, sigma=s)
+        torch.cuda.synchronize()
+        assert_close(y.cpu().numpy(), ref)
