@@ -283,11 +283,18 @@ class SpmmPlan(BatchPlan):
     """One CSR matrix with k right-hand sides, X, Y, alpha and beta given per
     call: Y = alpha*A*X + beta*Y (sblas_batch_spmm_xy).  The structure is
     fixed at construction; the values may be replaced per call (val=, same
-    dtype as at construction)."""
+    dtype as at construction).
+
+    k = 16 products run as two k = 8 passes over the column halves of X and
+    Y (row stride 16): the k = 16 kernel needs 216 registers per thread and
+    keeps only 8 warps per SM, the k = 8 one 126; measured on a 1M-row
+    power-law matrix, forward 1.13 -> 1.08 ms and A^T G 1.35 -> 1.22 ms.
+    split16=False keeps the single k = 16 pass."""
 
     def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
                  n: int, k: int, s: int = 0, row_ids: torch.Tensor | None = None,
-                 m_out: int | None = None, val_perm: torch.Tensor | None = None):
+                 m_out: int | None = None, val_perm: torch.Tensor | None = None,
+                 split16: bool = True):
         dev = _require_cuda(rowptr, col, val, row_ids, val_perm)
         m = rowptr.numel() - 1 if m_out is None else int(m_out)
         # placeholders fixing the shapes; every call passes its own X and Y
@@ -296,6 +303,16 @@ class SpmmPlan(BatchPlan):
         super().__init__([(rowptr, col, val, row_ids, val_perm)], [xs[:n]], [ys[:m]], k, s=s)
         self.m, self.n = m, n
         self.val_dtype = None if val is None else val.dtype
+        self._half = None
+        if k == 16 and split16:
+            self._half = SpmmPlan(rowptr, col, val, n, 8, s=s, row_ids=row_ids, m_out=m_out,
+                                  val_perm=val_perm)
+
+    def close(self) -> None:
+        if getattr(self, "_half", None) is not None:
+            self._half.close()
+            self._half = None
+        super().close()
 
     def _check_val(self, val):
         if val is None:
@@ -314,9 +331,18 @@ class SpmmPlan(BatchPlan):
             raise TypeError("x and y must be float64")
         if x.shape[0] != self.n or y.shape[0] != self.m:
             raise ValueError("x must be (n, k) and y (m, k)")
-        rc = _lib.load().sblas_batch_spmm_xy(self._h, _ptr(val), _ptr(x), self.k, _ptr(y),
-                                             self.k, float(alpha), float(beta),
-                                             _stream_ptr(self.device))
+        lib = _lib.load()
+        if self._half is not None and x.is_contiguous() and y.is_contiguous():
+            # two k = 8 passes: columns 0-7, then 8-15 (64 bytes on, row stride 16)
+            for off in (0, 64):
+                rc = lib.sblas_batch_spmm_xy(self._half._h, _ptr(val),
+                                             C.c_void_p(x.data_ptr() + off), 16,
+                                             C.c_void_p(y.data_ptr() + off), 16, float(alpha),
+                                             float(beta), _stream_ptr(self.device))
+                _lib.check(rc)
+            return y
+        rc = lib.sblas_batch_spmm_xy(self._h, _ptr(val), _ptr(x), self.k, _ptr(y), self.k,
+                                     float(alpha), float(beta), _stream_ptr(self.device))
         _lib.check(rc)
         return y
 
