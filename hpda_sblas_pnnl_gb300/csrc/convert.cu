@@ -29,21 +29,16 @@ __device__ __forceinline__ void rows_start_at(int prev, int cur, int m, long lon
     for (int r = max(prev + 1, 0); r <= cur && r <= m; ++r) rowptr[r] = (int)k;
 }
 
+// One nonzero per thread (row arrays that are not 16-byte aligned); an index
+// outside [0, m) or a decrease (unsorted input) writes nothing.
 __global__ void coo_rowptr_kernel(int m, long long nnz, const int *__restrict__ row,
-                                  int *__restrict__ rowptr, int *__restrict__ bad)
+                                  int *__restrict__ rowptr)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k <= nnz; k += stride) {
         const int prev = (k == 0) ? -1 : __ldg(row + k - 1);
         const int cur = (k == nnz) ? m : __ldg(row + k);
-        if (k < nnz && (cur < 0 || cur >= m)) {
-            if (bad) atomicExch(bad, 1);
-            continue;
-        }
-        if (cur < prev) {
-            if (bad) atomicExch(bad, 1);
-            continue;
-        }
+        if ((k < nnz && (cur < 0 || cur >= m)) || cur < prev) continue;
         // rows prev+1 .. cur start at k (row `cur` itself starts at k too)
         rows_start_at(prev, cur, m, k, rowptr);
     }
@@ -149,8 +144,7 @@ int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *row
         coo_rowptr_quad_kernel<<<grid_for(nnz / 4 + 1, 256), 256, 0, stream>>>(m, nnz, coo_row,
                                                                               rowptr);
     } else {
-        coo_rowptr_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(m, nnz, coo_row, rowptr,
-                                                                    nullptr);
+        coo_rowptr_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(m, nnz, coo_row, rowptr);
     }
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
