@@ -133,6 +133,26 @@ def powerlaw(m: int = 4_000_000, mean_deg: float = 17.5, alpha: float = 2.1, dma
     return CSR(m, m, rowptr, col, val), x
 
 
+def _row_sums(rowptr: torch.Tensor, v: torch.Tensor, rows_per_chunk: int = 1 << 16) -> torch.Tensor:
+    """Sum of v over each CSR row, as a padded per-row reduction over chunks of
+    rows: the summation order is fixed, so the sums are the same on every run
+    (a scatter-add on the GPU accumulates in whatever order its atomics land)."""
+    m = rowptr.numel() - 1
+    out = torch.zeros(m, dtype=v.dtype, device=v.device)
+    if m == 0 or v.numel() == 0:
+        return out
+    start = rowptr.to(torch.int64)
+    lens = start[1:] - start[:-1]
+    for r0 in range(0, m, rows_per_chunk):
+        r1 = min(m, r0 + rows_per_chunk)
+        ln = lens[r0:r1]
+        j = torch.arange(int(ln.max()), device=v.device)
+        ok = j[None, :] < ln[:, None]
+        idx = (start[r0:r1, None] + j[None, :]).clamp_(max=v.numel() - 1)
+        out[r0:r1] = torch.where(ok, v[idx], torch.zeros((), dtype=v.dtype, device=v.device)).sum(1)
+    return out
+
+
 def banded_fem(m: int = 2_000_000, per_row: int = 140, band: int = 20_000, offband: float = 0.01,
                seed: int = 3, device="cpu") -> tuple[CSR, torch.Tensor]:
     """FEM-like banded matrix: 3x3 dense blocks at random block columns within
@@ -168,8 +188,7 @@ def banded_fem(m: int = 2_000_000, per_row: int = 140, band: int = 20_000, offba
     r = torch.repeat_interleave(torch.arange(m, device=device),
                                 (rowptr[1:] - rowptr[:-1]).to(torch.int64))
     diag = col.to(torch.int64) == r
-    absrow = torch.zeros(m, dtype=torch.float64, device=device)
-    absrow.index_add_(0, r, torch.where(diag, torch.zeros_like(val), val.abs()))
+    absrow = _row_sums(rowptr, torch.where(diag, torch.zeros_like(val), val.abs()))
     val = torch.where(diag, 1.0 + absrow[r], val)
     x = torch.randn(m, generator=g, dtype=torch.float64, device=device)
     return CSR(m, m, rowptr, col, val), x
