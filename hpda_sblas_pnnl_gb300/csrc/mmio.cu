@@ -1,7 +1,7 @@
 // MatrixMarket reading (host code only): the NIST mmio entry points the
-// reference's drivers call (include/mmio.h of the reference declares them;
+// reference's test programs call (include/mmio.h of the reference declares them;
 // their implementation is not vendored there) and a multi-threaded reader of
-// a whole coordinate file, the replacement of the drivers' per-entry fscanf
+// a whole coordinate file, the replacement of those programs' per-entry fscanf
 // loop (test/dspmv_test_dgx1.cu:133-181).
 //
 // The whole-file reader maps the file, splits its data section into one

@@ -62,7 +62,7 @@ def read_coo(path, expand: bool = False):
         lines = f.read().split("\n")
     code = read_banner(lines[0])
     if code[1] != "C" or code[2] == "C":
-        raise MMError("unsupported type")   # the drivers read real, integer, pattern only
+        raise MMError("unsupported type")   # the reference's test programs read real, integer, pattern only
     k = 1
     while k < len(lines) and (not lines[k].strip() or lines[k].lstrip().startswith("%")):
         k += 1

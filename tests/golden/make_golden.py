@@ -61,7 +61,7 @@ def main():
     rng = np.random.default_rng(20261203)
 
     # 1. the reference's 'g' matrix at n = 200 (test/dspmv_test_smt.cu:176-232),
-    #    x = 1, alpha = 1, beta = 0, y0 = 0 as in the drivers (:356-373, :446-458)
+    #    x = 1, alpha = 1, beta = 0, y0 = 0 as in the test programs (:356-373, :446-458)
     r, c, v = O.gen_g(200)
     val, rowptr, col = O.coo2csr(200, 200, v, r, c)
     save_case("g200", 200, 200, rowptr, col, val, np.ones(200), np.zeros(200), 1.0, 0.0)
