@@ -91,7 +91,7 @@ SBLAS_API int sblas_mm_read_header(const char *path, sblas_mm_header *h);
 
 /* Reads the entries of a coordinate file into COO arrays, 0-based, in file
  * order, using nthreads host threads (0: all cores).  The results equal the
- * reference drivers' loop (test/dspmv_test_dgx1.cu:160-181): rows and
+ * reference's test programs' loop (test/dspmv_test_dgx1.cu:160-181): rows and
  * columns minus one; real values as strtod reads them (fscanf "%lg");
  * integer values converted to double; pattern values 1.0; the first nnz
  * entries of the file (later lines ignored; fewer is an error).
