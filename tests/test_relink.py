@@ -5,7 +5,8 @@ include/mmio.h, linked to libsblas_gb300.so and run through paths that need
 no GPU (argument errors, host helpers, MatrixMarket banners).  Where the
 reference's source tree is present, its unchanged test programs
 (test/dspmv_test_{smt,dgx1,dgx2}.cu) are compiled and linked against this
-library with the command INTEGRATION.md gives."""
+library with the documented build command (nvcc, this repository's include
+directory first, -lsblas_gb300 alone)."""
 import os
 import shutil
 import subprocess
@@ -31,7 +32,7 @@ int main(int argc, char **argv)
     struct spmv_ret r = spMV_mgpu_baseline(3, 3, 5, &alpha, val, rowptr, col, x, &beta, y, 2);
     printf("%g %g %g %g %g\n", r.numa_part_time, r.part_time, r.comp_time, r.comm_time,
            r.merg_time);
-    printf("%s\n", sblas_last_error());
+    printf("%s|%d\n", sblas_last_error(), sblas_last_status());
     printf("%g %g %g\n", y[0], y[1], y[2]);
     printf("%d %d %d\n", get_row_from_index(3, rowptr, 0), get_row_from_index(3, rowptr, 2),
            get_row_from_index(3, rowptr, 4));
@@ -43,6 +44,17 @@ int main(int argc, char **argv)
     fclose(f);
     printf("%d %d %c%c%c%c %d %d %d %d\n", rc, rc2, t[0], t[1], t[2], t[3], M, N, nz,
            mm_is_symmetric(t) ? 1 : 0);
+    f = fopen(argv[2], "r");
+    rc = mm_read_banner(f, &t);
+    rc2 = mm_read_mtx_array_size(f, &M, &N);
+    fclose(f);
+    printf("%d %d %d %d %d\n", rc, rc2, mm_is_array(t) ? 1 : 0, M, N);
+    double pv[5] = {0.1, -2.5e-7, 123456789.0, 3.0, -0.0};
+    int iv[3] = {-1, 0, 2147483647};
+    print_vec_double(pv, 5, "d");
+    print_vec_int(iv, 3, "i");
+    print_vec_int(iv, 0, "none");
+    printf("%s\n", sblas_version());
     return 0;
 }
 """
@@ -71,6 +83,7 @@ int main(int argc, char **argv)
 """
 
 MTX = "%%MatrixMarket matrix coordinate real symmetric\n% comment\n3 3 2\n1 1 1.0\n3 1 2.0\n"
+MTX_ARRAY = "%%MatrixMarket matrix array real general\n%\n2 3\n1\n2\n3\n4\n5\n6\n"
 
 
 def _tool(name):
@@ -94,15 +107,25 @@ def test_c_caller_links_and_gets_statuses(sblas_lib, tmp_path):
                     str(exe), *_link_flags(lib_dir)], check=True)
     mtx = tmp_path / "a.mtx"
     mtx.write_text(MTX)
-    out = subprocess.run([str(exe), str(mtx)], check=True, capture_output=True,
+    arr = tmp_path / "b.mtx"
+    arr.write_text(MTX_ARRAY)
+    out = subprocess.run([str(exe), str(mtx), str(arr)], check=True, capture_output=True,
                          text=True).stdout.splitlines()
     assert out[0] == "-1 -1 -1 -1 -1"                 # failure record, no exit
-    assert "ngpu" in out[1]
+    msg, status = out[1].rsplit("|", 1)
+    assert "ngpu" in msg and int(status) == -2        # SBLAS_ERR_ARG
     assert out[2] == "7 8 9"                          # y untouched on failure
     rp = np.array([0, 2, 2, 5], dtype=np.int32)
     from hpda_sblas_pnnl_gb300 import api
     assert out[3] == " ".join(str(api.get_row_from_index(3, rp, i)) for i in (0, 2, 4))
     assert out[4] == "0 0 MCRS 3 3 2 1"
+    assert out[5] == "0 0 1 2 3"
+    # the reference's print_vec: "<s>: " then each value and a space (ostream
+    # defaults, i.e. %g for doubles)
+    assert out[6] == "d: " + "".join("%g " % v for v in (0.1, -2.5e-7, 123456789.0, 3.0, -0.0))
+    assert out[7] == "i: -1 0 2147483647 "
+    assert out[8] == "none: "
+    assert out[9].startswith("sblas-gb300")
 
 
 def test_cxx_caller_uses_member_functions_and_check_macro(sblas_lib, tmp_path):
@@ -116,6 +139,7 @@ def test_cxx_caller_uses_member_functions_and_check_macro(sblas_lib, tmp_path):
     ok = subprocess.run([str(exe)], check=True, capture_output=True, text=True)
     lines = ok.stdout.splitlines()
     assert lines[0] == "0,0,0,3,1"                    # numa_part, part, comm, comp, merg
+    assert lines[1] == "v: 4 5 6 "
     assert lines[-1] == "after"
     bad = subprocess.run([str(exe), "fail"], capture_output=True, text=True)
     assert bad.returncode != 0 and "after" not in bad.stdout
