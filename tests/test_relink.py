@@ -113,7 +113,7 @@ def test_c_caller_links_and_gets_statuses(sblas_lib, tmp_path):
                          text=True).stdout.splitlines()
     assert out[0] == "-1 -1 -1 -1 -1"                 # failure record, no exit
     msg, status = out[1].rsplit("|", 1)
-    assert "ngpu" in msg and int(status) == -2        # SBLAS_ERR_ARG
+    assert "ngpu" in msg and int(status) == -2        # SBLAS_ERR_NGPU
     assert out[2] == "7 8 9"                          # y untouched on failure
     rp = np.array([0, 2, 2, 5], dtype=np.int32)
     from hpda_sblas_pnnl_gb300 import api
