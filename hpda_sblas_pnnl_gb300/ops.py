@@ -39,6 +39,18 @@ def _require_cuda(*ts: torch.Tensor | None) -> torch.device:
     return dev
 
 
+def _require_dtype(what: str, t: torch.Tensor | None, dtype: torch.dtype) -> None:
+    if t is not None and t.dtype != dtype:
+        raise TypeError(f"{what} must be {dtype} (got {t.dtype})")
+
+
+def _require_len(what: str, t: torch.Tensor | None, need: int) -> None:
+    """The kernels take bare pointers: an array shorter than the sizes say
+    would be read past its end on the device."""
+    if t is not None and t.numel() < need:
+        raise ValueError(f"{what} holds {t.numel()} elements, {need} needed")
+
+
 def workspace_bytes(nnz: int, sigma: int = 0) -> int:
     return int(_lib.load().sblas_tile_workspace_bytes(nnz, sigma))
 
@@ -81,6 +93,7 @@ def csrmv(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, x: 
         n = x.numel()
     if y.numel() != m or x.numel() < n:
         raise ValueError("shape mismatch")
+    _require_len("val", val, nnz)
     wb = work.numel() * work.element_size() if work is not None else 0
     lib = _lib.load()
     with torch.cuda.device(dev):
@@ -95,13 +108,22 @@ def coomv(row: torch.Tensor, col: torch.Tensor, val: torch.Tensor, x: torch.Tens
           y: torch.Tensor, alpha: float = 1.0, beta: float = 0.0, n: int | None = None,
           rowptr_work: torch.Tensor | None = None, sigma: int = 0) -> torch.Tensor:
     """y = alpha*A*x + beta*y with A in row-sorted COO (int32)."""
-    dev = _require_cuda(row, col, val, x, y)
+    dev = _require_cuda(row, col, val, x, y, rowptr_work)
+    for what, t, dt in (("row", row, torch.int32), ("col", col, torch.int32),
+                        ("val", val, torch.float64), ("x", x, torch.float64),
+                        ("y", y, torch.float64), ("rowptr_work", rowptr_work, torch.int32)):
+        _require_dtype(what, t, dt)
     m = y.numel()
+    n = n if n is not None else x.numel()
+    _require_len("row", row, col.numel())
+    _require_len("val", val, col.numel())
+    _require_len("x", x, n)
+    _require_len("rowptr_work", rowptr_work, m + 1)
     if rowptr_work is None:
         rowptr_work = torch.empty(m + 1, dtype=torch.int32, device=dev)
     lib = _lib.load()
     with torch.cuda.device(dev):
-        rc = lib.sblas_dcoomv(m, n if n is not None else x.numel(), col.numel(), float(alpha),
+        rc = lib.sblas_dcoomv(m, n, col.numel(), float(alpha),
                               _ptr(val), _ptr(row), _ptr(col), _ptr(x), float(beta), _ptr(y),
                               _ptr(rowptr_work), sigma, C.c_void_p(0), 0, _stream_ptr(dev))
     _lib.check(rc)
@@ -112,7 +134,12 @@ def csc_to_csr(m: int, n: int, colptr: torch.Tensor, rowidx: torch.Tensor,
                val: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """Device CSC -> CSR (stable; columns ascending inside each row)."""
     dev = _require_cuda(colptr, rowidx, val)
+    _require_dtype("colptr", colptr, torch.int32)
+    _require_dtype("rowidx", rowidx, torch.int32)
+    _require_dtype("val", val, torch.float64)
     nnz = rowidx.numel()
+    _require_len("colptr", colptr, n + 1)
+    _require_len("val", val, nnz)
     lib = _lib.load()
     wb = int(lib.sblas_csc_to_csr_workspace_bytes(m, n, nnz))
     work = torch.empty(max(wb, 1), dtype=torch.uint8, device=dev)
@@ -148,6 +175,9 @@ class CsrPlan:
     def __init__(self, rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None,
                  n: int | None = None, kernel: int = KERNEL_MERGEPATH, sigma: int = 0):
         dev = _require_cuda(rowptr, col, val)
+        _require_dtype("rowptr", rowptr, torch.int32)
+        _require_dtype("col", col, torch.int32)
+        _require_len("val", val, col.numel())
         if kernel not in (KERNEL_MERGEPATH, KERNEL_CSR5):
             raise ValueError("plans use the tile kernels (2 or 3)")
         lib = _lib.load()
@@ -178,7 +208,13 @@ class CsrPlan:
 
     def __call__(self, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0,
                  beta: float = 0.0) -> torch.Tensor:
+        if _require_cuda(x, y) != self.device:
+            raise ValueError("x and y must be on the plan's device")
+        _require_dtype("x", x, torch.float64)
+        _require_dtype("y", y, torch.float64)
         n = self.n if self.n is not None else x.numel()
+        if y.numel() != self.m or x.numel() < n:
+            raise ValueError("shape mismatch")
         lib = _lib.load()
         rc = lib.sblas_dcsrmv_analysed(self.kernel, self.m, n, self.nnz, float(alpha),
                                        _ptr(self.val), self.vk, _ptr(self.rowptr), _ptr(self.col),
@@ -244,6 +280,8 @@ class BatchPlan:
                 raise ValueError(f"matrix {i}: row_ids must be int32 with one entry per row")
             if vperm is not None and (vperm.dtype != torch.int32 or vperm.numel() != col.numel()):
                 raise ValueError(f"matrix {i}: val_perm must be int32 with one entry per nonzero")
+            if vperm is None:
+                _require_len(f"matrix {i}: val", val, col.numel())
             if (y.shape[0] != m if rid is None else y.shape[0] < m) or \
                     (x.dim() > 1 and x.shape[1] != self.k) or \
                     (y.dim() > 1 and y.shape[1] != self.k) or (self.k > 1 and x.dim() != 2):
@@ -329,8 +367,11 @@ class SpmmPlan(BatchPlan):
         self._check_val(val)
         if x.dtype != torch.float64 or y.dtype != torch.float64:
             raise TypeError("x and y must be float64")
-        if x.shape[0] != self.n or y.shape[0] != self.m:
+        if x.shape[0] != self.n or y.shape[0] != self.m or x.numel() != self.n * self.k or \
+                y.numel() != self.m * self.k:
             raise ValueError("x must be (n, k) and y (m, k)")
+        if _require_cuda(x, y) != self.device:
+            raise ValueError("x and y must be on the plan's device")
         lib = _lib.load()
         if self._half is not None and x.is_contiguous() and y.is_contiguous():
             # two k = 8 passes: columns 0-7, then 8-15 (64 bytes on, row stride 16)
@@ -351,8 +392,11 @@ class SpmmPlan(BatchPlan):
         _require_cuda(g, x, dval)
         if g.dtype != torch.float64 or x.dtype != torch.float64:
             raise TypeError("g and x must be float64")
-        if g.shape[0] != self.m or x.shape[0] != self.n or dval.dtype != self.val_dtype:
-            raise ValueError("g must be (m, k), x (n, k), dval of the values' dtype")
+        if g.shape[0] != self.m or x.shape[0] != self.n or dval.dtype != self.val_dtype or \
+                g.numel() != self.m * self.k or x.numel() != self.n * self.k or \
+                dval.numel() != self.matrices[0][1].numel():
+            raise ValueError("g must be (m, k), x (n, k), dval one value per stored entry "
+                             "of the values' dtype")
         rc = _lib.load().sblas_batch_sddmm(self._h, _ptr(g), self.k, _ptr(x), self.k, _ptr(dval),
                                            _stream_ptr(self.device))
         _lib.check(rc)
@@ -372,6 +416,9 @@ def csr_transpose(m: int, n: int, rowptr: torch.Tensor,
     """Device CSR structure of A^T: (t_rowptr, t_col, perm) with the values of
     A^T equal to val[perm]."""
     dev = _require_cuda(rowptr, col)
+    _require_dtype("rowptr", rowptr, torch.int32)
+    _require_dtype("col", col, torch.int32)
+    _require_len("rowptr", rowptr, m + 1)
     nnz = col.numel()
     lib = _lib.load()
     wb = int(lib.sblas_csr_transpose_workspace_bytes(m, n, nnz))
@@ -389,6 +436,9 @@ def csr_transpose(m: int, n: int, rowptr: torch.Tensor,
 def gather_values(val: torch.Tensor, perm: torch.Tensor, out: torch.Tensor) -> torch.Tensor:
     """out[p] = val[perm[p]] on the device (FP64 or FP32 values)."""
     dev = _require_cuda(val, perm, out)
+    _require_dtype("perm", perm, torch.int32)
+    _require_dtype("out", out, val.dtype)
+    _require_len("out", out, perm.numel())
     rc = _lib.load().sblas_gather_values(perm.numel(), _val_kind(val), _ptr(val), _ptr(perm),
                                          _ptr(out), _stream_ptr(dev))
     _lib.check(rc)
@@ -403,8 +453,12 @@ def csr_filter_x(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | No
     dev = _require_cuda(rowptr, col, val, x)
     if val is not None and val.dtype != torch.float64:
         raise TypeError("val must be float64 or None")
+    _require_dtype("rowptr", rowptr, torch.int32)
+    _require_dtype("col", col, torch.int32)
+    _require_dtype("x", x, torch.float64)
     m = rowptr.numel() - 1
     nnz = col.numel()
+    _require_len("val", val, nnz)
     lib = _lib.load()
     wb = int(lib.sblas_csr_filter_x_workspace_bytes(nnz))
     work = torch.empty(max(wb, 1), dtype=torch.uint8, device=dev)
