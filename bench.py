@@ -183,7 +183,19 @@ def run_reference(args):
     from hpda_sblas_pnnl_gb300 import synth
     from oracle import oracle as O
     O.build() if not O.LIB.exists() else None
-    a, x = make_workload("cpu", args.seed, args.m)
+    # The same seeded matrix as the GPU arm: generated with the same device's
+    # random streams (torch's CPU and CUDA generators differ), then copied to
+    # host memory.  Only input generation touches the GPU; the timed loop is
+    # the reference's CPU code.
+    gen_dev = "cuda" if torch.cuda.is_available() else "cpu"
+    try:
+        a, x = make_workload(gen_dev, args.seed, args.m)
+        a, x = a.to("cpu"), x.cpu()
+    except (RuntimeError, torch.cuda.OutOfMemoryError):
+        gen_dev = "cpu"   # inputs only: same distribution, another random stream
+        a, x = make_workload(gen_dev, args.seed, args.m)
+    if torch.cuda.is_available():
+        torch.cuda.empty_cache()
     m, n, nnz = a.m, a.n, a.nnz
     a_np = tuple(np.ascontiguousarray(t) for t in a.numpy())
     x_np = np.ascontiguousarray(x.numpy())
@@ -204,7 +216,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded power-law stand-in for the reference's SuiteSparse graphs)",
         "config": {"workload": WORKLOAD, "m": m, "n": n, "nnz": nnz,
-                   "bytes_per_step": bytes_step, "host_threads": threads},
+                   "bytes_per_step": bytes_step, "host_threads": threads,
+                   "generated_on": gen_dev},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                          "kind": kind, "sample": sample,
                          "gflops": round(2 * nnz * len(ts) / total / 1e9, 3)},
