@@ -29,6 +29,9 @@ def test_reference_arm_small_case_prints_the_contract_line():
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["m"] == 20000
+    # inputs drawn where the GPU arm draws them when a GPU is present
+    import torch
+    assert d["config"]["generated_on"] == ("cuda" if torch.cuda.is_available() else "cpu")
 
 
 def test_reference_arm_other_ranks_exit_quietly():
