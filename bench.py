@@ -63,6 +63,9 @@ def parse():
                         "FEM-like generator, --m rows)")
     p.add_argument("--values", default="f64", choices=["f64", "f32"],
                    help="with --kernel-only: FP64 values or FP32 values (FP64 sums)")
+    p.add_argument("--mmio", type=int, default=0, metavar="NNZ",
+                   help="host only: time the MatrixMarket reader on a seeded coordinate file "
+                        "of NNZ real entries against the reference's per-entry fscanf loop")
     return p.parse_args()
 
 
@@ -669,10 +672,71 @@ def run_probe():
     print(json.dumps(out), flush=True)
 
 
+def run_mmio(args):
+    """--mmio NNZ: the library's MatrixMarket reader (sblas_mm_read_coo, all
+    host threads and one) against the reference's reading loop (one fscanf
+    per entry, test/dspmv_test_dgx1.cu:160-181, restated in the oracle) on a
+    seeded real coordinate file: 1M x 1M, uniform indices, N(0, 1) values
+    written with 17 significant digits.  The file is read from the page
+    cache (written just before); results must agree bit for bit."""
+    import tempfile
+
+    import numpy as np
+    from hpda_sblas_pnnl_gb300 import mmio
+    from oracle import oracle as O
+    O.build() if not O.LIB.exists() else None
+    nz, m = int(args.mmio), 1_000_000
+    rng = np.random.default_rng(args.seed)
+    with tempfile.TemporaryDirectory() as td:
+        path = Path(td) / "uniform_1m.mtx"
+        with open(path, "w") as f:
+            f.write("%%MatrixMarket matrix coordinate real general\n% seeded\n")
+            f.write(f"{m} {m} {nz}\n")
+            for s0 in range(0, nz, 1 << 20):
+                k = min(nz, s0 + (1 << 20)) - s0
+                r = rng.integers(1, m + 1, k)
+                c = rng.integers(1, m + 1, k)
+                v = rng.standard_normal(k)
+                f.write("".join("%d %d %.17g\n" % t for t in zip(r.tolist(), c.tolist(),
+                                                                  v.tolist())))
+        size = path.stat().st_size
+
+        def timed(fn, reps):
+            ts, out = [], None
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                out = fn()
+                ts.append(time.perf_counter() - t0)
+            return statistics.median(ts), out
+
+        threads = os.cpu_count() or 1
+        t_all, lib_all = timed(lambda: mmio.read_coo(path, threads=0), 3)
+        t_one, lib_one = timed(lambda: mmio.read_coo(path, threads=1), 2)
+        t_ref, ref = timed(lambda: O.mm_read_fscanf(path), 1)
+    same = all(a.tobytes() == b.tobytes() and a.tobytes() == c.tobytes()
+               for a, b, c in zip(lib_all[2:], lib_one[2:], ref[2:]))
+
+    def leg(t, nthreads):
+        return {"s": round(t, 4), "mb_s": round(size / t / 1e6, 1),
+                "m_entries_s": round(nz / t / 1e6, 2), "threads": nthreads}
+
+    print(json.dumps({
+        "mode": "mmio", "file_bytes": size, "nnz": nz,
+        "library_all_threads": leg(t_all, threads), "library_one_thread": leg(t_one, 1),
+        "reference_fscanf_loop": leg(t_ref, 1),
+        "speedup_vs_reference": round(t_ref / t_all, 2), "bit_identical": bool(same)}),
+        flush=True)
+    if not same:
+        sys.exit(1)
+
+
 def main():
     args = parse()
     if args.probe:
         run_probe()
+        return
+    if args.mmio:
+        run_mmio(args)
         return
     if args.impl == "reference":
         run_reference(args)

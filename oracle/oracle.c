@@ -12,7 +12,9 @@
  * the reference's own CPU code on the same inputs (checked against the
  * reference's own functions compiled from its sources: oracle/ref_build.sh).
  */
+#include <ctype.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
@@ -382,4 +384,66 @@ long long oracle_csr_filter_x(int m, const int *rowptr, const int *col, const do
         orowptr[i + 1] = (int)k;
     }
     return k;
+}
+
+/* The reference's reading of a coordinate MatrixMarket file
+ * (test/dspmv_test_dgx1.cu:133-181): the banner's type word, the size line
+ * after the '%' comment lines ("M N nz", as the NIST mm_read_mtx_crd_size
+ * reads it), then one fscanf per entry: "%d %d\n" for pattern files (value
+ * 1), "%d %d %lg\n" for real, "%d %d %d\n" for integer (converted to
+ * double), both indices minus one.  With row, col and val NULL only the
+ * header is read (*kind: 0 real, 1 integer, 2 pattern).  Returns 0, or -1
+ * when the file, its header or an entry cannot be read (the reference
+ * ignores fscanf's result; on well-formed files the two agree). */
+int oracle_mm_read_fscanf(const char *path, int *m, int *n, long long *nnz, int *kind,
+                          int *row, int *col, double *val)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    char line[1025];
+    if (!fgets(line, sizeof line, f) || strncmp(line, "%%MatrixMarket", 14) != 0) {
+        fclose(f);
+        return -1;
+    }
+    for (char *p = line; *p; ++p) *p = (char)tolower((unsigned char)*p);
+    *kind = strstr(line, "pattern") ? 2 : (strstr(line, "integer") ? 1 : 0);
+    do {
+        if (!fgets(line, sizeof line, f)) {
+            fclose(f);
+            return -1;
+        }
+    } while (line[0] == '%');
+    int mm = 0, nn = 0, nz = 0;
+    if (sscanf(line, "%d %d %d", &mm, &nn, &nz) != 3) {
+        fclose(f);
+        return -1;
+    }
+    *m = mm;
+    *n = nn;
+    *nnz = nz;
+    if (!row || !col || !val) {
+        fclose(f);
+        return 0;
+    }
+    for (int i = 0; i < nz; i++) {
+        int ok;
+        if (*kind == 2) {
+            ok = fscanf(f, "%d %d\n", &row[i], &col[i]) == 2;
+            val[i] = 1;
+        } else if (*kind == 0) {
+            ok = fscanf(f, "%d %d %lg\n", &row[i], &col[i], &val[i]) == 3;
+        } else {
+            int tmp = 0;
+            ok = fscanf(f, "%d %d %d\n", &row[i], &col[i], &tmp) == 3;
+            val[i] = tmp;
+        }
+        if (!ok) {
+            fclose(f);
+            return -1;
+        }
+        row[i]--;
+        col[i]--;
+    }
+    fclose(f);
+    return 0;
 }

@@ -52,6 +52,11 @@ void oracle_csr_sddmm(int m, int k, const int *rowptr, const int *col, const dou
 long long oracle_csr_filter_x(int m, const int *rowptr, const int *col, const double *val,
                               const double *x, int *orowptr, int *ocol, double *oval);
 
+/* test/dspmv_test_dgx1.cu:133-181: per-entry fscanf reading of a coordinate
+ * file (header query with NULL arrays). */
+int oracle_mm_read_fscanf(const char *path, int *m, int *n, long long *nnz, int *kind,
+                          int *row, int *col, double *val);
+
 #ifdef __cplusplus
 }
 #endif

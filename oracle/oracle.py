@@ -7,6 +7,7 @@ bench.py's CPU-baseline / reference arm, never by the product package.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -56,6 +57,10 @@ def _lib() -> C.CDLL:
                                         _dp]
         _o.oracle_csr_filter_x.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _ip, _ip, _dp]
         _o.oracle_csr_filter_x.restype = C.c_longlong
+        _o.oracle_mm_read_fscanf.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                             C.POINTER(C.c_longlong), C.POINTER(C.c_int), _ip,
+                                             _ip, _dp]
+        _o.oracle_mm_read_fscanf.restype = C.c_int
     return _o
 
 
@@ -215,6 +220,24 @@ def csr_filter_x(m, rowptr, col, val, x):
     k = _lib().oracle_csr_filter_x(m, _i(rowptr), _i(col), _d(val), _d(x), _i(orp), _i(oc),
                                    _d(ov))
     return orp, oc[:k].copy(), ov[:k].copy()
+
+
+def mm_read_fscanf(path):
+    """The reference's per-entry fscanf reading of a coordinate file
+    (test/dspmv_test_dgx1.cu:133-181) -> (m, n, row, col, val), 0-based.
+    Raises ValueError where that loop cannot read the file."""
+    lib = _lib()
+    p = os.fsencode(str(path))
+    m, n, kind, nnz = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+    args = (C.byref(m), C.byref(n), C.byref(nnz), C.byref(kind))
+    if lib.oracle_mm_read_fscanf(p, *args, None, None, None) != 0:
+        raise ValueError(f"{path}: unreadable MatrixMarket header")
+    row = np.empty(nnz.value, np.int32)
+    col = np.empty(nnz.value, np.int32)
+    val = np.empty(nnz.value, np.float64)
+    if lib.oracle_mm_read_fscanf(p, *args, _i(row), _i(col), _d(val)) != 0:
+        raise ValueError(f"{path}: an entry fscanf cannot read")
+    return m.value, n.value, row, col, val
 
 
 def coo2csc(m, n, val, row, col):

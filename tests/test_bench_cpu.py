@@ -1,6 +1,7 @@
 """The benchmark's host logic without a GPU: the reference arm's contract
-line, its behaviour on ranks other than 0, and the max-over-ranks timing of
-the multi-rank path on a two-process gloo group."""
+line, its behaviour on ranks other than 0, the MatrixMarket reader timing
+mode, and the max-over-ranks timing of the multi-rank path on a two-process
+gloo group."""
 import json
 import os
 import subprocess
@@ -32,6 +33,15 @@ def test_reference_arm_small_case_prints_the_contract_line():
     # inputs drawn where the GPU arm draws them when a GPU is present
     import torch
     assert d["config"]["generated_on"] == ("cuda" if torch.cuda.is_available() else "cpu")
+
+
+def test_mmio_mode_times_both_readers_and_checks_parity():
+    r = run_bench(["--mmio", "30000"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert d["mode"] == "mmio" and d["nnz"] == 30000 and d["bit_identical"] is True
+    for leg in ("library_all_threads", "library_one_thread", "reference_fscanf_loop"):
+        assert d[leg]["s"] > 0 and d[leg]["mb_s"] > 0
 
 
 def test_reference_arm_other_ranks_exit_quietly():

@@ -1,7 +1,8 @@
 """The MatrixMarket reader (include/mmio.h, csrc/mmio.cu) against the
 oracle's restatement of the reference drivers' reading loop
 (oracle/mmread.py: NIST banner and size line, then fscanf per entry,
-test/dspmv_test_dgx1.cu:139-181).  Indices and values bit for bit."""
+test/dspmv_test_dgx1.cu:139-181; for large files also the same loop in C,
+oracle_mm_read_fscanf).  Indices and values bit for bit."""
 import ctypes as C
 
 import numpy as np
@@ -105,6 +106,14 @@ def test_large_file_threads_agree(sblas_lib, tmp_path, field, sym):
         got = check_same(p, expand=(sym != "general"), threads=t)
         for x, y in zip(base, got):
             assert x.tobytes() == y.tobytes()
+    # the reference's own loop restated in C (fscanf per entry; no expansion)
+    from hpda_sblas_pnnl_gb300 import mmio
+    from oracle import oracle as O
+    fm, fn, fr, fc, fv = O.mm_read_fscanf(p)
+    mm, nn, rr, cc, vv = mmio.read_coo(p, expand_symmetric=False)
+    assert (fm, fn) == (mm, nn)
+    assert fr.tobytes() == rr.tobytes() and fc.tobytes() == cc.tobytes()
+    assert fv.tobytes() == vv.tobytes()
 
 
 def test_scipy_written_file(sblas_lib, tmp_path):
