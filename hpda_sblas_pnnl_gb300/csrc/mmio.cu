@@ -66,6 +66,32 @@ bool parse_ll(const char *tok, long long *v)
     return true;
 }
 
+// The next token of [p, e) read in place as a decimal integer, accepting
+// what strtoll (base 10) accepts as a whole token: an optional sign, then
+// one or more digits and nothing else up to the next whitespace; false on
+// any other character, no digits, or a value outside long long.  Indices
+// and integer values take this path (no copy, no errno, no locale); it was
+// a copy plus strtoll per token, the largest cost of parsing a line.
+bool scan_ll(const char *&p, const char *e, long long *v)
+{
+    while (p < e && is_space(*p)) ++p;
+    if (p >= e) return false;
+    const bool neg = (*p == '-');
+    if (*p == '+' || *p == '-') ++p;
+    const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
+    const char *d0 = p;
+    unsigned long long acc = 0;
+    bool over = false;
+    for (; p < e && *p >= '0' && *p <= '9'; ++p) {
+        const unsigned dig = (unsigned)(*p - '0');
+        if (acc > (lim - dig) / 10) over = true;
+        else acc = acc * 10 + dig;
+    }
+    if (p == d0 || over || (p < e && !is_space(*p))) return false;
+    *v = neg ? (long long)(0ull - acc) : (long long)acc;
+    return true;
+}
+
 bool parse_double(const char *tok, double *v)
 {
     char *end = nullptr;
@@ -394,14 +420,14 @@ int sblas_mm_read_coo(const char *path, int expand_symmetric, int nthreads, long
             long long r, c;
             double v = 1.0;
             const char *bad = nullptr;
-            if (!next_token(p, e, tok, sizeof tok) || !parse_ll(tok, &r)) bad = "row index";
-            else if (!next_token(p, e, tok, sizeof tok) || !parse_ll(tok, &c)) bad = "column index";
+            if (!scan_ll(p, e, &r)) bad = "row index";
+            else if (!scan_ll(p, e, &c)) bad = "column index";
             else if (r < 1 || r > m || c < 1 || c > n) bad = "index out of range";
             else if (field == 'R') {
                 if (!next_token(p, e, tok, sizeof tok) || !parse_double(tok, &v)) bad = "value";
             } else if (field == 'I') {
                 long long iv;
-                if (!next_token(p, e, tok, sizeof tok) || !parse_ll(tok, &iv)) bad = "value";
+                if (!scan_ll(p, e, &iv)) bad = "value";
                 else v = (double)iv;
             }
             if (bad) {

@@ -139,6 +139,10 @@ def test_scipy_written_file(sblas_lib, tmp_path):
     (BANNER.format("real", "general") + "3 3 2\n1 1\n2 2 2.0\n", -8, "value"),
     (BANNER.format("integer", "general") + "3 3 1\n1 1 2.5\n", -8, "value"),
     (BANNER.format("real", "general") + "3 x 2\n1 1 1.0\n", -8, "size"),
+    (BANNER.format("real", "general") + "3 3 1\n- 1 1.0\n", -8, "row index"),
+    (BANNER.format("real", "general") + "3 3 1\n1 2a 1.0\n", -8, "column index"),
+    (BANNER.format("real", "general") + "3 3 1\n+-1 1 1.0\n", -8, "row index"),
+    (BANNER.format("integer", "general") + "3 3 1\n1 1 1x\n", -8, "value"),
 ])
 def test_malformed_files_fail_with_status(sblas_lib, tmp_path, text, status, words):
     from hpda_sblas_pnnl_gb300 import _lib, mmio
@@ -148,6 +152,27 @@ def test_malformed_files_fail_with_status(sblas_lib, tmp_path, text, status, wor
     assert e.value.status == status and words in str(e.value), str(e.value)
     with pytest.raises(R.MMError):
         R.read_coo(p)
+
+
+def test_integer_tokens_read_in_place(sblas_lib, tmp_path):
+    """Indices and integer values as strtoll reads a whole token: signs,
+    leading zeros (past 64 characters too), the long long extremes as
+    values; a value beyond long long is refused."""
+    text = (BANNER.format("integer", "general") + "5 5 5\n"
+            "+1 1 -9223372036854775808\n"
+            "0002 +003 9223372036854775807\n"
+            + "0" * 70 + "4 5 -0\n"
+            "5\t\t5\v+17\n"
+            "1 5 000\n")
+    p = write(tmp_path, "ints.mtx", text)
+    rr, cc, vv = check_same(p)
+    assert rr.tolist() == [0, 1, 3, 4, 0] and cc.tolist() == [0, 2, 4, 4, 4]
+    assert vv.tolist() == [-2.0 ** 63, 2.0 ** 63, 0.0, 17.0, 0.0]
+    from hpda_sblas_pnnl_gb300 import _lib, mmio
+    p2 = write(tmp_path, "over.mtx", BANNER.format("integer", "general") +
+               "2 2 1\n1 1 9223372036854775808\n")
+    with pytest.raises(_lib.SblasError, match="value"):
+        mmio.read_coo(p2)
 
 
 def test_missing_file(sblas_lib, tmp_path):
