@@ -66,6 +66,9 @@ def parse():
     p.add_argument("--mmio", type=int, default=0, metavar="NNZ",
                    help="host only: time the MatrixMarket reader on a seeded coordinate file "
                         "of NNZ real entries against the reference's per-entry fscanf loop")
+    p.add_argument("--mmio-digits", type=int, default=17, choices=range(1, 18), metavar="D",
+                   help="with --mmio: significant digits of the written values (17: every "
+                        "double round-trips; 16 or fewer: the reader's exact short path)")
     return p.parse_args()
 
 
@@ -677,8 +680,9 @@ def run_mmio(args):
     host threads and one) against the reference's reading loop (one fscanf
     per entry, test/dspmv_test_dgx1.cu:160-181, restated in the oracle) on a
     seeded real coordinate file: 1M x 1M, uniform indices, N(0, 1) values
-    written with 17 significant digits.  The file is read from the page
-    cache (written just before); results must agree bit for bit."""
+    written with --mmio-digits significant digits (default 17).  The file is
+    read from the page cache (written just before); results must agree bit
+    for bit."""
     import tempfile
 
     import numpy as np
@@ -686,6 +690,7 @@ def run_mmio(args):
     from oracle import oracle as O
     O.build() if not O.LIB.exists() else None
     nz, m = int(args.mmio), 1_000_000
+    vfmt = "%d %d %." + str(int(args.mmio_digits)) + "g\n"
     rng = np.random.default_rng(args.seed)
     with tempfile.TemporaryDirectory() as td:
         path = Path(td) / "uniform_1m.mtx"
@@ -697,8 +702,7 @@ def run_mmio(args):
                 r = rng.integers(1, m + 1, k)
                 c = rng.integers(1, m + 1, k)
                 v = rng.standard_normal(k)
-                f.write("".join("%d %d %.17g\n" % t for t in zip(r.tolist(), c.tolist(),
-                                                                  v.tolist())))
+                f.write("".join(vfmt % t for t in zip(r.tolist(), c.tolist(), v.tolist())))
         size = path.stat().st_size
 
         def timed(fn, reps):
@@ -721,7 +725,7 @@ def run_mmio(args):
                 "m_entries_s": round(nz / t / 1e6, 2), "threads": nthreads}
 
     print(json.dumps({
-        "mode": "mmio", "file_bytes": size, "nnz": nz,
+        "mode": "mmio", "file_bytes": size, "nnz": nz, "value_digits": int(args.mmio_digits),
         "library_all_threads": leg(t_all, threads), "library_one_thread": leg(t_one, 1),
         "reference_fscanf_loop": leg(t_ref, 1),
         "speedup_vs_reference": round(t_ref / t_all, 2), "bit_identical": bool(same)}),

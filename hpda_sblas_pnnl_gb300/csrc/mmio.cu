@@ -92,6 +92,61 @@ bool scan_ll(const char *&p, const char *e, long long *v)
     return true;
 }
 
+// The decimal number [p, e) (one whole token) by Clinger's fast path (W. D.
+// Clinger, "How to Read Floating Point Numbers Accurately", PLDI 1990): the
+// token is W * 10^E with a decimal significand W <= 2^53 and |E| <= 22, so
+// W and 10^|E| are both exact doubles and one IEEE multiplication (E >= 0)
+// or division (E < 0) rounds once, to the double strtod returns.  Accepts
+// [sign] digits [. digits] [e|E [sign] digits] with at least one significand
+// digit; false for any other token (inf, nan, hexadecimal, 17 or more
+// significant digits -- W >= 10^16 > 2^53 --, W > 2^53, |E| > 22, other
+// characters): the caller then converts it with strtod.
+bool fast_double(const char *p, const char *e, double *v)
+{
+    static const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,
+                                      1e8,  1e9,  1e10, 1e11, 1e12, 1e13, 1e14, 1e15,
+                                      1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    bool neg = false;
+    if (p < e && (*p == '+' || *p == '-')) neg = (*p++ == '-');
+    unsigned long long w = 0;
+    int sig = 0, ndig = 0, scale = 0;
+    for (; p < e && *p >= '0' && *p <= '9'; ++p, ++ndig) {
+        if (w == 0 && *p == '0') continue;            // leading zeros
+        if (++sig > 16) return false;
+        w = w * 10 + (unsigned)(*p - '0');
+    }
+    if (p < e && *p == '.') {
+        for (++p; p < e && *p >= '0' && *p <= '9'; ++p, ++ndig) {
+            --scale;
+            if (w == 0 && *p == '0') continue;
+            if (++sig > 16) return false;
+            w = w * 10 + (unsigned)(*p - '0');
+        }
+    }
+    if (ndig == 0) return false;
+    if (p < e && (*p == 'e' || *p == 'E')) {
+        ++p;
+        bool eneg = false;
+        if (p < e && (*p == '+' || *p == '-')) eneg = (*p++ == '-');
+        const char *d0 = p;
+        int x = 0;
+        for (; p < e && *p >= '0' && *p <= '9'; ++p)
+            if ((x = x * 10 + (*p - '0')) > 9999) return false;
+        if (p == d0) return false;
+        scale += eneg ? -x : x;
+    }
+    if (p != e || w > (1ull << 53)) return false;
+    if (w == 0) {
+        *v = neg ? -0.0 : 0.0;
+        return true;
+    }
+    if (scale < -22 || scale > 22) return false;
+    const double d = static_cast<double>(w);
+    const double r = scale >= 0 ? d * kPow10[scale] : d / kPow10[-scale];
+    *v = neg ? -r : r;
+    return true;
+}
+
 bool parse_double(const char *tok, double *v)
 {
     char *end = nullptr;
@@ -424,7 +479,21 @@ int sblas_mm_read_coo(const char *path, int expand_symmetric, int nthreads, long
             else if (!scan_ll(p, e, &c)) bad = "column index";
             else if (r < 1 || r > m || c < 1 || c > n) bad = "index out of range";
             else if (field == 'R') {
-                if (!next_token(p, e, tok, sizeof tok) || !parse_double(tok, &v)) bad = "value";
+                while (p < e && is_space(*p)) ++p;
+                const char *t = p;
+                while (t < e && !is_space(*t)) ++t;
+                if (t > p && fast_double(p, t, &v)) {
+                    p = t;
+                } else if (t > p && t < data + len) {
+                    // strtod in place: the byte after the token is whitespace
+                    // inside the mapping, so the conversion stops there
+                    char *end = nullptr;
+                    v = std::strtod(p, &end);
+                    if (end != t) bad = "value";
+                    p = t;
+                } else if (!next_token(p, e, tok, sizeof tok) || !parse_double(tok, &v)) {
+                    bad = "value";
+                }
             } else if (field == 'I') {
                 long long iv;
                 if (!scan_ll(p, e, &iv)) bad = "value";

@@ -154,6 +154,33 @@ def test_malformed_files_fail_with_status(sblas_lib, tmp_path, text, status, wor
         R.read_coo(p)
 
 
+def test_real_values_of_every_digit_count(sblas_lib, tmp_path):
+    """Values of 1 to 17 significant digits, decimal exponents -30 to 30,
+    written in several forms (%g, %e, %f, leading '+', '.5', '5.', 'E'):
+    the reader's exact short-number path (Clinger) and its strtod path give
+    the same doubles as the Python and the C fscanf oracles, bit for bit."""
+    rng = np.random.default_rng(23)
+    vals = []
+    for digits in range(1, 18):
+        for ex in range(-30, 31, 3):
+            x = float(rng.uniform(1, 10)) * 10.0 ** ex * (-1) ** int(rng.integers(2))
+            vals += ["%.*g" % (digits, x), "%.*e" % (digits - 1, x), "%.*E" % (digits - 1, x)]
+    vals += ["%.6f" % float(v) for v in rng.standard_normal(50)]
+    vals += ["+1.5", ".5", "5.", "-.25e+3", "+0", "-0", "-0.0", "0e-400", "9007199254740992",
+             "9007199254740993", "1e22", "1e23", "1e-22", "123456789012345e-22",
+             "0.000000000000000000000000000001", "4.9406564584124654e-324", "inf", "-nan"]
+    vals = [v for v in vals if v not in ("inf", "-nan")]    # the Python oracle refuses these
+    lines = [BANNER.format("real", "general"), f"7 7 {len(vals)}\n"]
+    lines += [f"{1 + i % 7} {1 + (i // 7) % 7} {v}\n" for i, v in enumerate(vals)]
+    p = write(tmp_path, "digits.mtx", "".join(lines))
+    rr, cc, vv = check_same(p, threads=1)
+    check_same(p, threads=3)
+    from oracle import oracle as O
+    _, _, fr, fc, fv = O.mm_read_fscanf(p)
+    assert fv.tobytes() == vv.tobytes()
+    assert np.signbit(vv[vals.index("-0")]) and not np.signbit(vv[vals.index("+0")])
+
+
 def test_integer_tokens_read_in_place(sblas_lib, tmp_path):
     """Indices and integer values as strtoll reads a whole token: signs,
     leading zeros (past 64 characters too), the long long extremes as
