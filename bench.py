@@ -1,10 +1,10 @@
 """Benchmark of the FP64 SpMV hot path on GB300 (one JSON line on stdout).
 
 Workload (the power-law configuration): y = 1.0*A*x + 0.0*y, A a 4.0M x 4.0M
-power-law graph with 64.2M nonzeros (out-degree exponent 2.1, max row 20k),
+power-law graph with ~70M nonzeros (out-degree exponent 2.1, max row 20k),
 values 1.0 FP64, x ~ U(0,1), int32 CSR indices.  One step = one SpMV over
 the whole matrix through sblas_dcsrmv (tile partition + tile kernel + carry
-fix-up; 3 launches), inputs resident in HBM.  The compulsory bytes (851 MB:
+fix-up; 3 launches), inputs resident in HBM.  The compulsory bytes (~920 MB:
 val, col, rowptr, x read once, y written once) exceed the 129 MB L2, so no
 flush is needed between steps; x (32 MB) stays L2-resident by design.
 
@@ -35,7 +35,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "SpMV HBM GB/s & % roofline: plain FP64 vs mixed/batched/fwd+bwd at stated err"
-WORKLOAD = ("power-law graph 4.0M x 4.0M, 64.2M nnz (exponent 2.1, max row 20k), values 1.0 "
+WORKLOAD = ("power-law graph 4.0M x 4.0M, ~70M nnz (exponent 2.1, max row 20k), values 1.0 "
             "FP64, x~U(0,1); FP64 CSR y=1.0*A*x+0.0*y")
 FALLBACK_HBM = 6800.0
 
@@ -53,8 +53,6 @@ def parse():
     p.add_argument("--m", type=int, default=4_000_000,
                    help="rows of the power-law matrix (smaller only for profiling captures)")
     p.add_argument("--sigma", type=int, default=0, help="tile shape (0 = library default)")
-    p.add_argument("--probe", action="store_true",
-                   help="print the hardware ceilings (FP64 pipe, random gathers, HBM read)")
     p.add_argument("--kernel-only", action="store_true",
                    help="time the device steps only (no e2e, CPU baseline, extras): the "
                         "small case used for ncu captures")
@@ -342,8 +340,7 @@ def run_ours(args):
                 "bounds_note": "1 DFMA per nonzero at the measured 5.3e11 DFMA/s caps this matrix "
                                f"at {5.3e11 * bytes_step / nnz / 1e9:.0f} GB/s; one random L2 "
                                "gather per nonzero at the measured 2.8e11/s caps it at "
-                               f"{2.8e11 * bytes_step / nnz / 1e9:.0f} GB/s "
-                               "(profiles/probes_gb300.md)"}
+                               f"{2.8e11 * bytes_step / nnz / 1e9:.0f} GB/s"}
         traffic_file = ROOT / "profiles" / "traffic.json"
         if traffic_file.exists():
             try:
@@ -604,7 +601,7 @@ def run_autograd_extra(dev, stream, args):
     (dX = A^T G and dval), measured with CUDA events, FP64 and FP32 values."""
     import torch
     from hpda_sblas_pnnl_gb300 import autograd, synth
-    a, _ = synth.powerlaw(m=1_000_000, mean_deg=20.0, seed=args.seed + 5, device=dev,
+    a, _ = synth.powerlaw(m=1_000_000, mean_deg=22.4, seed=args.seed + 5, device=dev,
                           values="normal")
     k = 16
     g = torch.Generator(device=dev)
@@ -645,34 +642,6 @@ def run_autograd_extra(dev, stream, args):
         del op, val, x, y
         torch.cuda.empty_cache()
     return res
-
-
-def run_probe():
-    """The ceilings that bound FP64 SpMV on this GPU (library probes)."""
-    import ctypes as C
-    import torch
-    from hpda_sblas_pnnl_gb300 import _lib
-    torch.cuda.init()
-    lib = _lib.load(build_if_missing=True)
-    full, one, gps, bps = C.c_double(), C.c_double(), C.c_double(), C.c_double()
-    _lib.check(lib.sblas_probe_fp64(C.byref(full), C.byref(one)))
-    out = {"fp64_dfma_warp_instr_per_s_32_lanes": full.value,
-           "fp64_dfma_warp_instr_per_s_1_lane": one.value,
-           "fp64_dfma_lane_ops_per_s": 32 * full.value}
-    for rng in (4_000_000, 250_000, 16_384):
-        _lib.check(lib.sblas_probe_gather(rng, C.byref(gps)))
-        out[f"random_8B_gathers_per_s_range_{rng}"] = gps.value
-    # shared memory reserved per CTA (256 threads): the split of the SM's
-    # 256 KB between shared memory and L1 that the driver picks for the launch
-    occ = C.c_int()
-    sweep = {}
-    for kb in (0, 16, 24, 32, 40, 48, 56, 80, 100):
-        _lib.check(lib.sblas_probe_gather_smem(4_000_000, kb * 1024, C.byref(gps), C.byref(occ)))
-        sweep[f"{kb}KB_x{occ.value}"] = gps.value
-    out["random_8B_gathers_per_s_by_smem_per_cta_x_ctas_per_sm"] = sweep
-    _lib.check(lib.sblas_probe_stream(C.byref(bps)))
-    out["hbm_read_bytes_per_s"] = bps.value
-    print(json.dumps(out), flush=True)
 
 
 def run_mmio(args):
@@ -736,9 +705,6 @@ def run_mmio(args):
 
 def main():
     args = parse()
-    if args.probe:
-        run_probe()
-        return
     if args.mmio:
         run_mmio(args)
         return

@@ -53,6 +53,13 @@ class BatchMatrix(C.Structure):
     ]
 
 
+class NnzPart(C.Structure):
+    """include/sblas_gb300.h (sblas_nnz_part): one part of the v1 nnz split."""
+
+    _fields_ = [(f, C.c_int) for f in ("start_idx", "end_idx", "start_row", "end_row",
+                                        "start_flag", "end_flag", "m", "nnz")]
+
+
 class MMHeader(C.Structure):
     """include/mmio.h (sblas_mm_header): banner and size line of a file."""
 
@@ -75,6 +82,12 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_last_error": (C.c_char_p, []),
     "sblas_last_status": (C.c_int, []),
     "sblas_version": (C.c_char_p, []),
+    "sblas_stream_status": (C.c_int, [C.c_void_p, C.c_int]),
+    "sblas_nnz_partition": (C.c_int, [C.c_int, C.c_longlong, _ip, C.c_int, C.c_void_p]),
+    "sblas_part_rowptr": (C.c_int, [_ip, C.c_void_p, _ip]),
+    "sblas_merge_parts": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_double, _dp]),
+    "sblas_set_wait_limit_ns": (None, [C.c_ulonglong]),
+    "sblas_test_hold_producer": (None, [C.c_int]),
     "sblas_set_compat_mode": (None, [C.c_int]),
     "sblas_get_compat_mode": (C.c_int, []),
     "sblas_tile_workspace_bytes": (C.c_size_t, [C.c_longlong, C.c_int]),
@@ -92,10 +105,6 @@ SIGNATURES: dict[str, tuple] = {
     "sblas_noalloc_scratch_bytes": (C.c_size_t, []),
     "sblas_dcsrmv_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, _vp, _vp, _vp, _vp,
                                        C.c_double, _vp, _vp]),
-    "sblas_probe_fp64": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
-    "sblas_probe_gather": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
-    "sblas_probe_gather_smem": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double), _ip]),
-    "sblas_probe_stream": (C.c_int, [C.POINTER(C.c_double)]),
     "sblas_dcoomv": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, _vp, _vp, _vp,
                                C.c_double, _vp, _vp, C.c_int, _vp, C.c_size_t, _vp]),
     "sblas_csc_to_csr_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_longlong]),

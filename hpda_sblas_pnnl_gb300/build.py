@@ -55,7 +55,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
     nvcc = nvcc_path()
     objdir = LIBDIR / "obj"
     objdir.mkdir(parents=True, exist_ok=True)
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
                     "--expt-relaxed-constexpr", "-I", str(PKG.parent / "include")]
     flags += list(extra or [])
 

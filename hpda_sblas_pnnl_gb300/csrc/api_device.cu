@@ -108,6 +108,24 @@ const char *sblas_last_error(void) { return g_msg; }
 int sblas_last_status(void) { return g_status; }
 const char *sblas_version(void) { return "sblas-gb300 0.1 (sm_103a)"; }
 
+int sblas_stream_status(void *stream, int clear)
+{
+    clear_error();
+    int word = 0;
+    const int rc = tile_sticky_status(static_cast<cudaStream_t>(stream), clear != 0, &word);
+    if (rc != SBLAS_OK) return rc;
+    if (word != 0) {
+        set_error(SBLAS_ERR_TIMEOUT,
+                  "a tile kernel gave up a bounded wait (device word %d); its y is partial", word);
+        return SBLAS_ERR_TIMEOUT;
+    }
+    return SBLAS_OK;
+}
+
+void sblas_set_wait_limit_ns(unsigned long long ns) { set_wait_limit_ns(ns); }
+
+void sblas_test_hold_producer(int on) { set_test_stall(on); }
+
 void sblas_set_compat_mode(int mode) { g_compat = mode ? 1 : 0; }
 
 int sblas_get_compat_mode(void)

@@ -140,6 +140,21 @@ __global__ void rebase_rowptr_kernel(int count, const int *__restrict__ rp, int 
 
 constexpr long long kPipeMinNnz = 1LL << 22;   // smaller matrices: copy, then compute
 
+// After the call's stream has completed: false (with SBLAS_ERR_TIMEOUT set)
+// if a tile launch on workspace w gave up one of its bounded waits, which
+// leaves y partly written.
+bool launches_completed(const Call &c, void *w)
+{
+    int word = 0;
+    if (tile_workspace_status(w, &word) != SBLAS_OK) return false;
+    if (word != 0) {
+        set_error(SBLAS_ERR_TIMEOUT, "%s: the SpMV kernel gave up a bounded wait (device word "
+                  "%d); y is not valid", c.name, word);
+        return false;
+    }
+    return true;
+}
+
 // Large CSR calls with host arrays: the matrix travels in kPipeChunks row
 // chunks of equal nonzero counts, each chunk's SpMV starting as soon as its
 // values and columns have arrived (copies on the context's copy stream, the
@@ -214,6 +229,7 @@ spmv_ret run_host_pipelined(const Call &c, DeviceContext *ctx)
     DROPIN_CUDA(cudaStreamWaitEvent(ks, ctx->chunk_ev[0], 0));
     DROPIN_CUDA(cudaEventRecord(e2, ks));
     const double beta_eff = c.additive ? c.beta + 1.0 : c.beta;
+    bool status_cleared = false;
     for (int k = 0; k < K; ++k) {
         const int rows = r[k + 1] - r[k];
         if (rows == 0) continue;
@@ -225,10 +241,14 @@ spmv_ret run_host_pipelined(const Call &c, DeviceContext *ctx)
         DROPIN_CUDA(cudaStreamWaitEvent(ks, ctx->chunk_ev[1 + k], 0));
         const double *val = reinterpret_cast<const double *>(reinterpret_cast<unsigned char *>(d_val) + vo[k]);
         const int *col = reinterpret_cast<const int *>(reinterpret_cast<unsigned char *>(d_idx) + io[k]);
+        // the chunks share one workspace: its status word is cleared once,
+        // by the first launch, so a chunk that gave up a wait stays visible
         const int rc = (cnnz == 0)
                            ? launch_scale_y(rows, beta_eff, d_y + r[k], ks)
                            : launch_tile_spmv(rows, n, cnnz, c.alpha, val, SBLAS_VAL_F64, rp, col, d_x,
-                                              beta_eff, d_y + r[k], sigma, w, ks);
+                                              beta_eff, d_y + r[k], sigma, w, ks, false,
+                                              !status_cleared);
+        if (cnnz > 0) status_cleared = true;
         if (rc != SBLAS_OK) return failed();
         DROPIN_CUDA(cudaMemcpyAsync(c.y + r[k], d_y + r[k], sizeof(double) * (size_t)rows,
                                     cudaMemcpyDeviceToHost, ks));
@@ -236,6 +256,7 @@ spmv_ret run_host_pipelined(const Call &c, DeviceContext *ctx)
     DROPIN_CUDA(cudaEventRecord(e3, ks));
     const double tm = wall();
     DROPIN_CUDA(cudaEventSynchronize(e3));
+    if (!launches_completed(c, w)) return failed();
     spmv_ret ret = zero_ret();
     float t_comm = 0.f, t_comp = 0.f;
     DROPIN_CUDA(cudaEventElapsedTime(&t_comm, e0, e1));
@@ -332,6 +353,7 @@ spmv_ret run_host(Call c)
     // ---- the SpMV on rows [row_lo, row_hi)
     const int rows = c.row_hi - c.row_lo;
     const double beta_eff = c.additive ? c.beta + 1.0 : c.beta;
+    void *tile_work = nullptr;   // workspace of the tile launch, if one ran
     if (rows > 0) {
         // a row sub-range keeps absolute offsets into col/val
         const int *rp = rowptr + c.row_lo;
@@ -342,19 +364,21 @@ spmv_ret run_host(Call c)
         } else if (c.kernel == 1) {
             rc = launch_rowsplit_spmv(rows, n, nnz, c.alpha, val, rp, col, d_x, beta_eff, yp, st);
         } else {
-            const int sigma = (c.kernel == 3) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
-            void *w = device_scratch(0, tile_workspace_bytes(nnz, sigma));
-            if (!w) {
+            const int tile_sigma =
+                (c.kernel == 3) ? csr5_sigma_for(m, nnz) : default_sigma_for(m, nnz);
+            tile_work = device_scratch(0, tile_workspace_bytes(nnz, tile_sigma));
+            if (!tile_work) {
                 set_error(SBLAS_ERR_ALLOC, "%s: workspace allocation failed", c.name);
                 return failed();
             }
             rc = launch_tile_spmv(rows, n, nnz, c.alpha, val, SBLAS_VAL_F64, rp, col, d_x,
-                                  beta_eff, yp, sigma, w, st);
+                                  beta_eff, yp, tile_sigma, tile_work, st);
         }
         if (rc != SBLAS_OK) return failed();
     }
     DROPIN_CUDA(cudaEventRecord(e3, st));
     DROPIN_CUDA(cudaEventSynchronize(e3));
+    if (tile_work && !launches_completed(c, tile_work)) return failed();
     float t_comm = 0.f, t_part = 0.f, t_comp = 0.f;
     DROPIN_CUDA(cudaEventElapsedTime(&t_comm, e0, e1));
     DROPIN_CUDA(cudaEventElapsedTime(&t_part, e1, e2));

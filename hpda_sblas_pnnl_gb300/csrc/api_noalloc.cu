@@ -20,8 +20,18 @@
 //
 // Set-up: the first call on a device (with that device current) resolves the
 // array's device address with cudaGetSymbolAddress and creates the
-// library's per-device context (a CUDA stream and events, no device
-// memory).  Make that first call before any stream capture.
+// library's per-device context (a CUDA stream and events), and configures the
+// kernels the calls launch (loading them).  Under CUDA's
+// default lazy module loading that first call is also when the library's
+// module is loaded onto the device, and with it when the 7 MiB array gets
+// its device memory; with CUDA_MODULE_LOADING=EAGER the array is placed when
+// the library is loaded instead.  A call with m = 0 does the set-up and
+// nothing else: make one before entering a region where allocation is
+// forbidden, and before any stream capture.
+//
+// Failure detection: the kernels' bounded waits write the status word inside
+// the array and the library's sticky device word; sblas_stream_status
+// reports a wait that gave up.
 #include <mutex>
 
 #include "sblas_internal.h"
@@ -59,6 +69,9 @@ int noalloc_scratch(void **out)
             set_error(SBLAS_ERR_CUDA, "cannot create the per-device context");
             return SBLAS_ERR_CUDA;
         }
+        // load every kernel the calls launch now, not at the first real call
+        const int rc = tile_preload_f64(default_sigma_for(0, 0));
+        if (rc != SBLAS_OK) return rc;
         g_noalloc_ptr[dev] = p;
     }
     *out = g_noalloc_ptr[dev];
@@ -83,6 +96,9 @@ int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const double *val,
         set_error(SBLAS_ERR_ARG, "bad sizes m=%d n=%d nnz=%d", m, n, nnz);
         return SBLAS_ERR_ARG;
     }
+    void *scratch = nullptr;
+    const int rc = noalloc_scratch(&scratch);   // set-up on first use (m = 0: set-up only)
+    if (rc != SBLAS_OK) return rc;
     if (m == 0) return SBLAS_OK;
     if (y == nullptr || (nnz > 0 && (val == nullptr || rowptr == nullptr || col == nullptr ||
                                      x == nullptr))) {
@@ -98,9 +114,6 @@ int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const double *val,
                   nnz, need, kNoallocScratchBytes);
         return SBLAS_ERR_ARG;
     }
-    void *scratch = nullptr;
-    const int rc = noalloc_scratch(&scratch);
-    if (rc != SBLAS_OK) return rc;
     return launch_tile_spmv(m, n, nnz, alpha, val, SBLAS_VAL_F64, rowptr, col, x, beta, y, sigma,
                             scratch, static_cast<cudaStream_t>(stream));
 }

@@ -1,6 +1,6 @@
 // MatrixMarket reading (host code only): the NIST mmio entry points the
-// reference's test programs call (include/mmio.h of the reference declares them;
-// their implementation is not vendored there) and a multi-threaded reader of
+// reference's test programs call (the reference vendors them header-only in its
+// include/mmio.h: declarations and bodies) and a multi-threaded reader of
 // a whole coordinate file, the replacement of those programs' per-entry fscanf
 // loop (test/dspmv_test_dgx1.cu:133-181).
 //

@@ -28,9 +28,9 @@ int last_status();
 
 // ---- nnz-tile engine (the load-balanced CSR kernel) ----------------------
 // A tile is TILE_THREADS * sigma consecutive nonzeros.  Workspace per call:
+//   status[1]             device error flag (bounded waits), first 256 bytes
 //   row_part[ntiles + 1]  first owned row of every tile (int32)
 //   carry[ntiles]         FP64 partial of the row that continues past the tile
-//   status[1]             device error flag (bounded waits)
 struct TileShape {
     int threads;   // threads per CTA
     int sigma;     // nonzeros per thread
@@ -52,10 +52,25 @@ enum ValueKind { VAL_F64 = 0, VAL_F32 = 1, VAL_PATTERN = 2 };
 // `work` must hold tile_workspace_bytes(nnz, sigma) bytes, 256-byte aligned.
 // analysed = true: the partition of `work` was computed by
 // launch_tile_analyse for this row pointer and sigma (skipped here).
+// reset_status = false keeps the workspace's status word as it is (a call
+// made of several launches on one workspace clears it once, at its start).
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
                      int val_kind, const int *rowptr, const int *col, const double *x,
                      double beta, double *y, int sigma, void *work, cudaStream_t stream,
-                     bool analysed = false);
+                     bool analysed = false, bool reset_status = true);
+// Status word of a tile workspace (0 = every wait completed), read with a
+// synchronous copy: the caller has synchronised the launches' stream.
+int tile_workspace_status(void *work, int *out);
+// The sticky per-device word (any tile launch that gave up a wait), read
+// after `stream` completes; clear = reset it to 0.
+int tile_sticky_status(cudaStream_t stream, bool clear, int *out);
+// Bounded-wait limit of the tile kernels (0 = the default, 2 s) and the
+// test hook that keeps the producer warp from staging (waits then run out).
+// Configures (under lazy module loading: loads) every kernel of an FP64
+// tile SpMV of shape sigma on the current device.
+int tile_preload_f64(int sigma);
+void set_wait_limit_ns(unsigned long long ns);
+void set_test_stall(int on);
 int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void *work,
                         cudaStream_t stream);
 

@@ -36,8 +36,10 @@
 //    bit-reproducible run to run);
 //  * x is gathered with an L2 evict-last hint; grids are persistent
 //    (occupancy x SM count), tiles round-robin over CTAs.
+#include <atomic>
 #include <cstdio>
 #include <climits>
+#include <mutex>
 
 #include "ptx.cuh"
 #include "sblas_internal.h"
@@ -47,10 +49,21 @@ namespace sblas {
 namespace {
 
 constexpr int STAGES = 2;
-constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait, then error flag
+constexpr uint64_t DEFAULT_WAIT_NS = 2000000000ull;  // 2 s per wait, then error flag
 
 // Device error codes written to status[0].
 constexpr int DEV_ERR_TIMEOUT = 1;
+
+// Sticky per-device error word: every launch whose bounded wait gave up ORs
+// its code in, whatever workspace it ran with; read (and cleared) by
+// sblas_stream_status for the asynchronous entry points.
+__device__ int g_sticky_error;
+
+// Wait limit of the compute and epilogue warps and of the producer's wait
+// for a free stage (the producer's final wait for its own copies always
+// uses DEFAULT_WAIT_NS), and the test hook that holds the producer back.
+std::atomic<unsigned long long> g_wait_ns{DEFAULT_WAIT_NS};
+std::atomic<int> g_stall{0};
 
 __host__ __device__ constexpr size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
@@ -164,7 +177,16 @@ struct TileArgs {
     int *status;          // [1]
     int use_tma;          // val and col 16-byte aligned: bulk copies
     int rp_tma;           // rowptr 16-byte aligned: bulk copies of its tile slices
+    int stall;            // test hook: the producer stages nothing, every wait runs out
+    uint64_t wait_ns;     // limit of one bounded wait
 };
+
+// A bounded wait gave up: the launch's status word and the sticky word.
+__device__ __forceinline__ void report_timeout(const TileArgs &a)
+{
+    atomicExch(a.status, DEV_ERR_TIMEOUT);
+    atomicOr(&g_sticky_error, DEV_ERR_TIMEOUT);
+}
 
 // y epilogue for one finished row value v.
 template <int AB>
@@ -290,12 +312,12 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
     for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
         const int s = i % STAGES;
         const int p = i & 1;
-        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), WAIT_LIMIT_NS);
+        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), a.wait_ns);
         if (i >= 2)
             ok = ok && ptx::mbar_wait_bounded(sm.cempty(p), (uint32_t)(((i - 2) / 2) & 1),
-                                              WAIT_LIMIT_NS);
+                                              a.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            if (lane == 0) report_timeout(a);
             return;
         }
         const int *meta = sm.meta(s);
@@ -442,6 +464,7 @@ template <int SIGMA, int VK>
 __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
                                               int lane, uint64_t pol_stream)
 {
+    if (a.stall) return;   // test hook: nothing is staged, the other warps' waits run out
     int issued[STAGES];
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) issued[s] = 0;
@@ -459,9 +482,9 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
         const int R0 = __ldg(a.row_part + nt);
         const int R1 = __ldg(a.row_part + nt + 1);
         const bool ok = ptx::mbar_wait_bounded(sm.empty(s), (uint32_t)((i / STAGES) & 1),
-                                               WAIT_LIMIT_NS);
+                                               a.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            if (lane == 0) report_timeout(a);
             break;
         }
         ptx::fence_proxy_async_smem();
@@ -469,10 +492,12 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
         ++issued[s];
     }
     // the CTA may exit only when no copy into its shared memory is in flight
+    // (always the full limit: these copies are this warp's own and complete)
     if (lane == 0) {
         for (int s = 0; s < STAGES; ++s)
             if (issued[s] > 0)
-                ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((issued[s] - 1) & 1), WAIT_LIMIT_NS);
+                ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((issued[s] - 1) & 1),
+                                       DEFAULT_WAIT_NS);
     }
 }
 
@@ -497,9 +522,9 @@ __device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGM
          i += 2, tile += 2 * (int)gridDim.x) {
         const int p = i & 1;
         const bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1),
-                                               WAIT_LIMIT_NS);
+                                               a.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) atomicExch(a.status, DEV_ERR_TIMEOUT);
+            if (lane == 0) report_timeout(a);
             break;
         }
         const int *cm = sm.cmeta(p);
@@ -741,30 +766,54 @@ __global__ void scale_y_kernel(int m, double beta, double *__restrict__ y)
 constexpr int kSigmas[] = {11, 15, 19, 23, 27};
 constexpr int kNumSigmas = sizeof(kSigmas) / sizeof(kSigmas[0]);
 
+// Per device: the kernel's shared-memory attribute, set once, and its
+// resident CTAs per SM (0 = not configured yet); host threads may launch
+// concurrently.  Configuring also loads the kernel onto the device under
+// lazy module loading.
+template <int SIGMA, int VK, int AB>
+int configure_shape(int *out_bps)
+{
+    using L = Layout<SIGMA, VK>;
+    auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> blocks_per_sm[kMaxDev];
+    static std::mutex config_mu;
+    int dev = 0;
+    SBLAS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDev) {
+        set_error(SBLAS_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+        return SBLAS_ERR_UNSUPPORTED;
+    }
+    int bps = blocks_per_sm[dev].load(std::memory_order_acquire);
+    if (bps == 0) {
+        std::lock_guard<std::mutex> lk(config_mu);
+        bps = blocks_per_sm[dev].load(std::memory_order_acquire);
+        if (bps == 0) {
+            SBLAS_CUDA_TRY(cudaFuncSetAttribute(
+                kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::TOTAL));
+            SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA_THREADS,
+                                                                         L::TOTAL));
+            if (bps < 1) {
+                set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
+                          SIGMA);
+                return SBLAS_ERR_UNSUPPORTED;
+            }
+            blocks_per_sm[dev].store(bps, std::memory_order_release);
+        }
+    }
+    *out_bps = bps;
+    return SBLAS_OK;
+}
+
 template <int SIGMA, int VK, int AB>
 int launch_shape(const TileArgs &a, cudaStream_t stream)
 {
     using L = Layout<SIGMA, VK>;
     auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
-    static int configured_dev = -1;
-    static int blocks_per_sm = 0;
-    int dev = 0;
-    SBLAS_CUDA_TRY(cudaGetDevice(&dev));
-    if (configured_dev != dev) {
-        SBLAS_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)L::TOTAL));
-        int bps = 0;
-        SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA_THREADS,
-                                                                     L::TOTAL));
-        if (bps < 1) {
-            set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
-                      SIGMA);
-            return SBLAS_ERR_UNSUPPORTED;
-        }
-        blocks_per_sm = bps;
-        configured_dev = dev;
-    }
-    const int grid = min(a.ntiles, blocks_per_sm * device_num_sms());
+    int bps = 0;
+    const int rc = configure_shape<SIGMA, VK, AB>(&bps);
+    if (rc != SBLAS_OK) return rc;
+    const int grid = min(a.ntiles, bps * device_num_sms());
     kfn<<<grid, CTA_THREADS, L::TOTAL, stream>>>(a);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
@@ -804,12 +853,17 @@ int tile_shape_index(int sigma)
 
 static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// Workspace layout: the status word (first 256 bytes, at the same place
+// whatever the matrix, so launches of different sizes on one workspace share
+// it), then the tile partition, then the tile carries.
+constexpr size_t kStatusBytes = 256;
+
 size_t tile_workspace_bytes(long long nnz, int sigma)
 {
     const long long tile = (long long)TC * sigma;
     const long long ntiles = (nnz + tile - 1) / tile;
-    return align256(sizeof(int) * (size_t)(ntiles + 1)) + align256(sizeof(double) * (size_t)ntiles) +
-           256;
+    return kStatusBytes + align256(sizeof(int) * (size_t)(ntiles + 1)) +
+           align256(sizeof(double) * (size_t)ntiles);
 }
 
 int default_sigma_for(int m, long long nnz)
@@ -865,7 +919,7 @@ int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void
         return SBLAS_ERR_ARG;
     }
     const int ntiles = (int)ntiles_ll;
-    int *part = static_cast<int *>(work);
+    int *part = reinterpret_cast<int *>(static_cast<unsigned char *>(work) + kStatusBytes);
     const int threads = 256;
     if ((reinterpret_cast<uintptr_t>(rowptr) & 15) == 0) {
         const int quads = m / 4 + 1;
@@ -881,9 +935,73 @@ int launch_tile_analyse(int m, long long nnz, const int *rowptr, int sigma, void
     return SBLAS_OK;
 }
 
+// Status word of a tile workspace (after the partition and the carries).
+static int *status_in(void *work) { return static_cast<int *>(work); }
+
+int tile_workspace_status(void *work, int *out)
+{
+    *out = 0;
+    if (work == nullptr) return SBLAS_OK;
+    SBLAS_CUDA_TRY(cudaMemcpy(out, status_in(work), sizeof(int), cudaMemcpyDeviceToHost));
+    return SBLAS_OK;
+}
+
+int tile_sticky_status(cudaStream_t stream, bool clear, int *out)
+{
+    *out = 0;
+    SBLAS_CUDA_TRY(cudaMemcpyFromSymbolAsync(out, g_sticky_error, sizeof(int), 0,
+                                             cudaMemcpyDeviceToHost, stream));
+    SBLAS_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (clear && *out != 0) {
+        const int zero = 0;
+        SBLAS_CUDA_TRY(cudaMemcpyToSymbolAsync(g_sticky_error, &zero, sizeof(int), 0,
+                                               cudaMemcpyHostToDevice, stream));
+        SBLAS_CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+    return SBLAS_OK;
+}
+
+// Configures (and so loads) every kernel an FP64 SpMV of tile shape sigma
+// may launch on the current device.
+int tile_preload_f64(int sigma)
+{
+    int bps = 0, rc = SBLAS_OK;
+    switch (sigma) {
+#define SBLAS_PRELOAD(S)                                                            \
+    case S:                                                                         \
+        rc = configure_shape<S, VAL_F64, 0>(&bps);                                  \
+        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 1>(&bps);              \
+        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 2>(&bps);              \
+        break;
+        SBLAS_PRELOAD(11)
+        SBLAS_PRELOAD(15)
+        SBLAS_PRELOAD(19)
+        SBLAS_PRELOAD(23)
+        SBLAS_PRELOAD(27)
+#undef SBLAS_PRELOAD
+    default:
+        set_error(SBLAS_ERR_UNSUPPORTED, "sigma %d is not a compiled tile shape", sigma);
+        return SBLAS_ERR_UNSUPPORTED;
+    }
+    if (rc != SBLAS_OK) return rc;
+    cudaFuncAttributes fa;
+    SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, tile_partition_kernel));
+    SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, tile_partition_quad_kernel));
+    SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, tile_fixup_kernel));
+    SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, scale_y_kernel));
+    return SBLAS_OK;
+}
+
+void set_wait_limit_ns(unsigned long long ns)
+{
+    g_wait_ns.store(ns == 0 ? DEFAULT_WAIT_NS : ns, std::memory_order_relaxed);
+}
+
+void set_test_stall(int on) { g_stall.store(on ? 1 : 0, std::memory_order_relaxed); }
+
 int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val, int val_kind,
                      const int *rowptr, const int *col, const double *x, double beta, double *y,
-                     int sigma, void *work, cudaStream_t stream, bool analysed)
+                     int sigma, void *work, cudaStream_t stream, bool analysed, bool reset_status)
 {
     if (m <= 0) return SBLAS_OK;
     if (nnz <= 0) return launch_scale_y(m, beta, y, stream);
@@ -899,11 +1017,11 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     }
     const int ntiles = (int)ntiles_ll;
     unsigned char *w = static_cast<unsigned char *>(work);
-    int *part = reinterpret_cast<int *>(w);
-    double *carry = reinterpret_cast<double *>(w + align256(sizeof(int) * (size_t)(ntiles + 1)));
-    int *status = reinterpret_cast<int *>(w + align256(sizeof(int) * (size_t)(ntiles + 1)) +
-                                          align256(sizeof(double) * (size_t)ntiles));
-    SBLAS_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
+    int *part = reinterpret_cast<int *>(w + kStatusBytes);
+    double *carry = reinterpret_cast<double *>(w + kStatusBytes +
+                                               align256(sizeof(int) * (size_t)(ntiles + 1)));
+    int *status = status_in(work);
+    if (reset_status) SBLAS_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
     if (!analysed) {
         const int rc = launch_tile_analyse(m, nnz, rowptr, sigma, work, stream);
         if (rc != SBLAS_OK) return rc;
@@ -926,6 +1044,8 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     const uintptr_t vb = reinterpret_cast<uintptr_t>(val), cb = reinterpret_cast<uintptr_t>(col);
     a.use_tma = ((val_kind == VAL_PATTERN || (vb & 15) == 0) && (cb & 15) == 0) ? 1 : 0;
     a.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
+    a.stall = g_stall.load(std::memory_order_relaxed);
+    a.wait_ns = g_wait_ns.load(std::memory_order_relaxed);
     int rc = SBLAS_OK;
     switch (sigma) {
     case 11: rc = launch_vk<11>(val_kind, a, stream); break;

@@ -482,3 +482,14 @@ def spmspv(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None, x:
     device arrays: the filter and the product both run on the GPU."""
     orp, ocol, oval = csr_filter_x(rowptr, col, val, x)
     return csrmv(orp, ocol, oval, x, y, alpha, beta, n=x.numel(), kernel=kernel)
+
+
+def check_device(device: torch.device | None = None, clear: bool = True) -> None:
+    """Waits for the current stream of `device`, then raises SblasError
+    (SBLAS_ERR_TIMEOUT) if a tile kernel launched on that device gave up one
+    of its bounded waits since the last check: the y of that launch is only
+    partly written.  clear=True resets the device's sticky word."""
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    with torch.cuda.device(dev):
+        rc = _lib.load().sblas_stream_status(_stream_ptr(dev), 1 if clear else 0)
+    _lib.check(rc)

@@ -102,12 +102,15 @@ def _pareto_xmin(alpha: float, dmax: int, mean: float) -> float:
     return 0.5 * (lo + hi)
 
 
-def powerlaw(m: int = 4_000_000, mean_deg: float = 17.5, alpha: float = 2.1, dmax: int = 20_000,
+def powerlaw(m: int = 4_000_000, mean_deg: float = 19.1, alpha: float = 2.1, dmax: int = 20_000,
              seed: int = 2021, device="cpu", values: str = "ones") -> tuple[CSR, torch.Tensor]:
     """Power-law graph (m x m): out-degrees ~ discrete Pareto with exponent
     alpha clipped to [1, dmax], scaled to mean_deg; endpoints by a
     preferential-attachment stand-in (Zipf popularity over randomly permuted
     column ids, exponent 1/(alpha-1), which gives power-law in-degrees).
+    Duplicate endpoints are merged, so the stored nonzeros fall short of
+    m * mean_deg: at m = 4M the default mean_deg of 19.1 draws ~76M and keeps
+    ~70M (the benchmark size).
     values='ones' (binary pattern, 1.0) or 'normal' (N(0, 1)); x ~ U(0, 1)."""
     g = _gen(seed, device)
     xmin = _pareto_xmin(alpha, dmax, mean_deg)

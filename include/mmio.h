@@ -4,9 +4,11 @@
  * The reference's drivers read their matrices with the NIST MatrixMarket
  * I/O routines declared in its include/mmio.h (mm_read_banner,
  * mm_read_mtx_crd_size, mm_typecode_to_str and the mm_is_* queries; used at
- * test/dspmv_test_dgx1.cu:133-181, dspmv_test_dgx2.cu, dspmv_test_smt.cu),
- * whose implementation file the reference does not vendor.  This header
- * keeps that interface (the MM_typecode layout, query macros, error codes
+ * test/dspmv_test_dgx1.cu:133-181, dspmv_test_dgx2.cu, dspmv_test_smt.cu).
+ * The reference vendors them header-only: its include/mmio.h holds the
+ * declarations and the function bodies (mm_read_banner at :254,
+ * mm_read_mtx_crd_size at :339), compiled into every driver that includes
+ * it.  This header keeps that interface (the MM_typecode layout, query macros, error codes
  * and signatures are the published NIST ones, so a driver compiles
  * unchanged) with C linkage, implemented by the library.
  *

@@ -38,6 +38,7 @@ extern "C" {
 #define SBLAS_ERR_KERNEL (-6)         /* a kernel reported a device-side error */
 #define SBLAS_ERR_UNSUPPORTED (-7)    /* option not compiled in this build */
 #define SBLAS_ERR_FORMAT (-8)         /* malformed input file (MatrixMarket reader) */
+#define SBLAS_ERR_TIMEOUT (-9)        /* a kernel gave up a bounded wait; its output is partial */
 
 /* kernel versions, numbered as the reference's `kernel` argument
  * (src/dspmv_mgpu_v1.cu:256-278) */
@@ -56,6 +57,25 @@ SBLAS_API const char *sblas_last_error(void);
 SBLAS_API int sblas_last_status(void);
 /* Library version string. */
 SBLAS_API const char *sblas_version(void);
+
+/* Device-side failures of the asynchronous entry points.  Every wait inside
+ * the tile kernels is bounded (2 s by default); a launch that gives up a wait
+ * stops early, leaves y partly written and records it in a sticky per-device
+ * word.  This call waits for `stream` to complete, then returns SBLAS_OK or
+ * SBLAS_ERR_TIMEOUT if any tile launch on the current device gave up a wait
+ * since the word was last cleared (clear != 0 clears it).  The synchronous
+ * entry points (spmv_kernel.h) check their own launches and return failure
+ * themselves.  The reference has no counterpart: its checkCudaErrors prints
+ * and exits (include/detail/cuda/helper_cuda.h:583-595). */
+SBLAS_API int sblas_stream_status(void *stream, int clear);
+
+/* Testing hooks (process-wide; not for production use).  The wait limit of
+ * the tile kernels in nanoseconds (0 restores the default, 2 s), and a switch
+ * that keeps the tile kernels' producer warp from staging any tile, so that
+ * every launch's waits run out after the limit and report SBLAS_ERR_TIMEOUT:
+ * the way tests exercise the failure path without faulting the GPU. */
+SBLAS_API void sblas_set_wait_limit_ns(unsigned long long ns);
+SBLAS_API void sblas_test_hold_producer(int on);
 
 /* Reference-compatibility switches for the drop-in entry points (0 = off,
  * the default: every entry point computes y = alpha*A*x + beta*y on all rows).
@@ -119,25 +139,17 @@ SBLAS_API int sblas_dcsrmv_analysed(int kernel, int m, int n, long long nnz, dou
  * matrices (about 0.86 G nonzeros and up) fail with SBLAS_ERR_ARG.  The
  * array is shared by every call: calls that overlap on the GPU race.  The
  * first call on a device resolves the array's address and creates the
- * library's per-device context (no device memory): make it before any
- * stream capture.  Device arrays, stream-ordered on `stream`. */
+ * library's per-device context (a stream and events); under CUDA's default
+ * lazy module loading it is also when the library's module, and with it the
+ * 7 MiB array, is placed in device memory (CUDA_MODULE_LOADING=EAGER places
+ * it when the library loads).  A call with m = 0 does only that set-up:
+ * make one before entering a region that forbids allocation, and before any
+ * stream capture.  A bounded wait that gave up is reported by
+ * sblas_stream_status.  Device arrays, stream-ordered on `stream`. */
 SBLAS_API size_t sblas_noalloc_scratch_bytes(void);
 SBLAS_API int sblas_dcsrmv_noalloc(int m, int n, int nnz, double alpha, const double *val,
                                    const int *rowptr, const int *col, const double *x,
                                    double beta, double *y, void *stream);
-
-/* Hardware probes (diagnostics; allocate their own buffers and synchronise):
- * FP64 DFMA warp instructions per second with 32 and with 1 active lane;
- * random 8-byte gathers per second from a vector of `range` doubles;
- * streaming HBM read bytes per second. */
-SBLAS_API int sblas_probe_fp64(double *warp_instr_per_s_full, double *warp_instr_per_s_one_lane);
-SBLAS_API int sblas_probe_gather(int range, double *gathers_per_s);
-/* The gather probe with smem_per_cta bytes of (unused) shared memory per CTA
- * of 256 threads and as many CTAs per SM as fit (*ctas_per_sm): shows how
- * the shared-memory / L1 split the driver picks bounds random gathers. */
-SBLAS_API int sblas_probe_gather_smem(int range, int smem_per_cta, double *gathers_per_s,
-                                      int *ctas_per_sm);
-SBLAS_API int sblas_probe_stream(double *bytes_per_s);
 
 /* Row-sorted COO: builds the CSR row pointer on the device (atomic-free),
  * then runs the tile kernel.  rowptr_work: int[m + 1] device buffer. */
@@ -244,6 +256,37 @@ SBLAS_API int sblas_csr_filter_x(int m, long long nnz, const int *rowptr, const 
 /* dst[p] = src[perm[p]] for nnz values of the given kind (FP64 or FP32). */
 SBLAS_API int sblas_gather_values(long long nnz, int val_kind, const void *src, const int *perm,
                                   void *dst, void *stream);
+/* ---- decomposition across devices (host code, no GPU) -------------------
+ * The reference's nnz-balanced split of spMV_mgpu_v1 (src/dspmv_mgpu_v1.cu:
+ * 120-152 cut points, :183-193 part row pointers, :304-319 merge) for a
+ * caller that runs each part on its own device (one process per GPU) and
+ * exchanges the parts' results itself.  Given the same per-part results the
+ * merged y equals the reference's bit for bit. */
+typedef struct sblas_nnz_part {
+    int start_idx;    /* first nonzero of the part */
+    int end_idx;      /* last nonzero of the part (inclusive, as the reference) */
+    int start_row;    /* row holding start_idx */
+    int end_row;      /* row holding end_idx */
+    int start_flag;   /* 1: start_row begins in an earlier part (split row) */
+    int end_flag;     /* 1: end_row continues in a later part */
+    int m;            /* rows of the part: end_row - start_row + 1 */
+    int nnz;          /* nonzeros of the part: end_idx - start_idx + 1 */
+} sblas_nnz_part;
+
+/* Cuts nnz = rowptr[m] nonzeros into nparts equal ranges (nnz >= nparts). */
+SBLAS_API int sblas_nnz_partition(int m, long long nnz, const int *rowptr, int nparts,
+                                  sblas_nnz_part *parts);
+/* Row pointer of one part, part->m + 1 entries: 0, the inner rows rebased to
+ * the part's first nonzero, part->nnz.  The part's columns and values are
+ * col + start_idx and val + start_idx. */
+SBLAS_API int sblas_part_rowptr(const int *rowptr, const sblas_nnz_part *part, int *out);
+/* Merges the parts' results (part_y[d]: part d's m rows of
+ * alpha*A_d*x + beta*y0) into y, which holds y0 on entry: rows copied in part
+ * order, a split row gets the earlier parts' value added back and one
+ * beta*y0 removed. */
+SBLAS_API int sblas_merge_parts(int nparts, const sblas_nnz_part *parts,
+                                const double *const *part_y, double beta, double *y);
+
 /* Zero `bytes` bytes of device memory at p, stream-ordered (cudaMemsetAsync). */
 SBLAS_API int sblas_zero(void *p, size_t bytes, void *stream);
 

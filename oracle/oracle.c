@@ -192,6 +192,25 @@ int oracle_find_last_in_sorted(const int *a, int n, int key)
  * unsplit product (the decomposition the GPU kernels apply inside one GPU).
  * Returns 0, or -1 when a part would be empty (nnz < nparts), a case the
  * reference does not handle. */
+/* The v1 partition alone (src/dspmv_mgpu_v1.cu:120-152): for part i,
+ * out[7i .. 7i+6] = start_idx, end_idx, start_row, end_row, start_flag,
+ * end_flag, dev_m.  Returns -1 when nparts <= 0 or nnz < nparts. */
+int oracle_nnz_partition(int m, int nnz, const int *rowptr, int nparts, int *out)
+{
+    if (nparts <= 0 || nnz < nparts) return -1;
+    for (int i = 0; i < nparts; i++) {
+        int *o = out + 7 * i;
+        o[0] = (int)floor((double)((long long)i * nnz) / nparts);
+        o[1] = (int)floor((double)((long long)(i + 1) * nnz) / nparts) - 1;
+        o[2] = oracle_get_row_from_index(m, rowptr, o[0]);
+        o[3] = oracle_get_row_from_index(m, rowptr, o[1]);
+        o[4] = o[0] > rowptr[o[2]];
+        o[5] = o[1] < rowptr[o[3] + 1] - 1;
+        o[6] = o[3] - o[2] + 1;
+    }
+    return 0;
+}
+
 int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
                               const double *val, const int *rowptr, const int *col,
                               const double *x, const double *beta, double *y,

@@ -30,6 +30,7 @@ int oracle_get_row_from_index(int n, const int *a, int idx);
 int oracle_find_first_in_sorted(const int *a, int n, int key);
 int oracle_find_last_in_sorted(const int *a, int n, int key);
 
+int oracle_nnz_partition(int m, int nnz, const int *rowptr, int nparts, int *out);
 int oracle_csr_spmv_nnz_split(int m, int n, int nnz, const double *alpha,
                               const double *val, const int *rowptr, const int *col,
                               const double *x, const double *beta, double *y,

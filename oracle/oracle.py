@@ -42,6 +42,8 @@ def _lib() -> C.CDLL:
         _o.oracle_csr_spmv_omp.argtypes = spmv_args + [C.c_int]
         _o.oracle_csr_spmv_nnz_split.argtypes = spmv_args + [C.c_int]
         _o.oracle_csr_spmv_nnz_split.restype = C.c_int
+        _o.oracle_nnz_partition.argtypes = [C.c_int, C.c_int, _ip, C.c_int, _ip]
+        _o.oracle_nnz_partition.restype = C.c_int
         _o.oracle_get_row_from_index.argtypes = [C.c_int, _ip, C.c_int]
         _o.oracle_find_first_in_sorted.argtypes = [_ip, C.c_int, C.c_int]
         _o.oracle_find_last_in_sorted.argtypes = [_ip, C.c_int, C.c_int]
@@ -176,6 +178,17 @@ def csr_spmv_nnz_split(m, n, rowptr, col, val, x, y, nparts, alpha=1.0, beta=0.0
     if rc != 0:
         raise ValueError("nnz < nparts")
     return y
+
+
+def nnz_partition(m, rowptr, nparts):
+    """The reference's v1 split (src/dspmv_mgpu_v1.cu:120-152): an
+    (nparts, 7) int array of start_idx, end_idx, start_row, end_row,
+    start_flag, end_flag, rows per part."""
+    nnz = int(rowptr[m]) if m > 0 else 0
+    out = np.zeros((max(nparts, 1), 7), np.int32)
+    if _lib().oracle_nnz_partition(m, nnz, _i(rowptr), nparts, _i(out)) != 0:
+        raise ValueError("nnz < nparts")
+    return out
 
 
 def get_row_from_index(n, a, idx):

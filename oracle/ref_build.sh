@@ -8,10 +8,14 @@
 # The CUDA / cuSPARSE calls elsewhere in those files compile against the
 # host-only stand-in headers in oracle/ref_shim/ and are never executed.  The
 # reference's GPU path (cuSPARSE csrmv / csrmv_mp, CSR5) does not build with
-# CUDA 13 and is not compiled.  Usage: oracle/ref_build.sh [REFERENCE_ROOT]
+# CUDA 13 and is not compiled.
+# Usage: oracle/ref_build.sh [REFERENCE_ROOT]; the root is the argument, else
+# $SBLAS_REFERENCE_DIR, else the read-only location this recipe is run
+# against in the build container.  The root used is recorded in
+# oracle/_ref/REFERENCE_DIR for the tests that compile the reference's drivers.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${SBLAS_REFERENCE_DIR:-/root/reference}}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/test/dspmv_test_smt.cu" ]; then
   echo "reference sources not found under $REF; skipping oracle/_ref" >&2
@@ -29,4 +33,5 @@ $CXX $FLAGS -c "$REF/src/spmv_helper.cu" -o "$OUT/helper.o"
 $CXX -O2 -fPIC -fopenmp -ffp-contract=off -c "$HERE/ref_shim/ref_entry.cpp" -o "$OUT/entry.o"
 $CXX -shared -fopenmp -o "$OUT/libref_cpu.so" "$OUT/smt.o" "$OUT/dgx1.o" "$OUT/helper.o" "$OUT/entry.o"
 rm -f "$OUT"/*.o
+printf '%s\n' "$REF" > "$OUT/REFERENCE_DIR"
 echo "built $OUT/libref_cpu.so"

@@ -25,7 +25,7 @@ def rel_l2(y, ref):
 def powerlaw(cuda):
     from hpda_sblas_pnnl_gb300 import synth
     a, x = synth.powerlaw(device=cuda)
-    assert 60e6 < a.nnz < 80e6
+    assert 68e6 < a.nnz < 72e6          # ~70M after duplicate endpoints are merged
     return a, x
 
 

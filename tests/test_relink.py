@@ -18,7 +18,21 @@ import pytest
 from conftest import ROOT
 
 INC = ROOT / "include"
-REFERENCE = Path(os.environ.get("SBLAS_REFERENCE_DIR", "/root/reference"))
+
+
+def _reference_root() -> Path | None:
+    """The reference's source tree: $SBLAS_REFERENCE_DIR, else the root that
+    oracle/ref_build.sh compiled from (recorded in oracle/_ref/REFERENCE_DIR)."""
+    env = os.environ.get("SBLAS_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    rec = ROOT / "oracle" / "_ref" / "REFERENCE_DIR"
+    if rec.exists():
+        return Path(rec.read_text().strip())
+    return None
+
+
+REFERENCE = _reference_root()
 
 C_CALLER = r"""
 #include <stdio.h>
@@ -146,7 +160,7 @@ def test_cxx_caller_uses_member_functions_and_check_macro(sblas_lib, tmp_path):
     assert "CUDA error 35" in bad.stderr and "checkCudaErrors" not in bad.stderr
 
 
-@pytest.mark.skipif(not (REFERENCE / "test" / "dspmv_test_smt.cu").exists(),
+@pytest.mark.skipif(REFERENCE is None or not (REFERENCE / "test" / "dspmv_test_smt.cu").exists(),
                     reason="the reference's source tree is not present")
 def test_reference_test_programs_relink_unchanged(sblas_lib, tmp_path):
     """The reference's own test programs, unchanged, compile against this
