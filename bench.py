@@ -392,6 +392,9 @@ def run_ours(args):
         extras = {}
         if not args.no_extras:
             extras = run_extras(dev, stream, args)
+            if "powerlaw_csc" in extras:   # per-call CSC against the CSR step above
+                extras["powerlaw_csc"]["time_vs_csr_step"] = round(
+                    extras["powerlaw_csc"]["us"] / (ms_step * 1e3), 3)
 
         out = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": ws,
@@ -498,13 +501,36 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                                "gflops": round(2 * a.nnz / ms / 1e6, 1),
                                "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err,
                                "sigma": sg}
-    # CSC and COO (device conversion once, then the tile kernel; conversion timed apart)
+    # CSC: the inspector (row-ordered structure by the library's bucket sort)
+    # timed apart from the executor (values gathered into row order + tile
+    # kernel); the one-shot call (both) beside them
     colptr, rowidx, cval = synth.csr_to_csc(a)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rp2, c2, v2 = ops.csc_to_csr(a.m, a.n, colptr, rowidx, cval)
-    torch.cuda.synchronize()
-    conv_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(2):
+        plan_c = ops.CscPlan(a.m, colptr, rowidx)
+    insp_ms = statistics.mean(cuda_event_ms(
+        lambda: ops.CscPlan(a.m, colptr, rowidx), stream, 3))
+    for _ in range(3):
+        plan_c(cval, x, y)
+    csc_ms = statistics.mean(cuda_event_ms(lambda: plan_c(cval, x, y), stream, 10))
+    csc_err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+    cw = plan_c.work
+    for _ in range(2):
+        ops.cscmv(colptr, rowidx, cval, x, y, work=cw)
+    once_ms = statistics.mean(cuda_event_ms(
+        lambda: ops.cscmv(colptr, rowidx, cval, x, y, work=cw), stream, 3))
+    del plan_c, cw
+    bcsc = synth.compulsory_bytes(a.m, a.n, a.nnz, fmt="csc")
+    res["powerlaw_csc"] = {"gbs": round(bcsc / csc_ms / 1e6, 1),
+                           "gflops": round(2 * a.nnz / csc_ms / 1e6, 1),
+                           "frac": round(bcsc / csc_ms / 1e6 / pk, 4), "us": round(csc_ms * 1e3, 1),
+                           "rel_l2_err": csc_err, "inspector_us": round(insp_ms * 1e3, 1),
+                           "one_shot_us": round(once_ms * 1e3, 1),
+                           "note": "us/gbs: executor per call (values gathered into row order "
+                                   "+ tile kernel); inspector_us: row-ordered structure by the "
+                                   "library's bucket sort, once per pattern; one_shot_us: both "
+                                   "(sblas_dcscmv)"}
+    del colptr, rowidx, cval
+    torch.cuda.empty_cache()
     row = synth.csr_to_coo_rows(a)
     rpw = torch.empty(a.m + 1, dtype=torch.int32, device=dev)
     coo_ms = statistics.mean(cuda_event_ms(
@@ -514,7 +540,6 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                            "gflops": round(2 * a.nnz / coo_ms / 1e6, 1),
                            "frac": round(bcoo / coo_ms / 1e6 / pk, 4), "us": round(coo_ms * 1e3, 1),
                            "note": "row pointer built on device each call, then tile kernel"}
-    res["powerlaw_csc_to_csr_ms"] = round(conv_ms, 2)
     del a, x, y
     torch.cuda.empty_cache()
     return res
@@ -526,8 +551,9 @@ def run_batch_extra(dev, stream, args):
     k in {1, 4, 8} right-hand sides ~ U(-1, 1).  One graph-captured run of
     the batched plan (s picked by the autotuner) against 64 * k launches of
     the single-matrix tile kernel (one per matrix and right-hand side,
-    analysed plans, eager), both timed with CUDA events; agreement of the two
-    results (relative L2) is the correctness check at this size."""
+    analysed plans, eager), and for k >= 2 against 64 launches of the k-column
+    SpMM (one per matrix, ops.SpmmPlan), all timed with CUDA events; agreement
+    of the results (relative L2) is the correctness check at this size."""
     import numpy as np
     import torch
     from hpda_sblas_pnnl_gb300 import ops, synth, tune
@@ -571,6 +597,22 @@ def run_batch_extra(dev, stream, args):
 
         per_matrix()
         p_ms = statistics.median(cuda_event_ms(per_matrix, stream, 5))
+        # the fair per-matrix arm for k >= 2: one k-column SpMM launch per
+        # matrix (ops.SpmmPlan: same kernel family, one gather of X per nonzero)
+        pm_spmm_ms = None
+        if k > 1:
+            splans = [ops.SpmmPlan(a.rowptr, a.col, a.val, n=a.n, k=k, s=s_best) for a in mats]
+            ysp = [torch.zeros((a.m, k), dtype=torch.float64, device=dev) for a in mats]
+
+            def per_matrix_spmm():
+                for sp, xx, yy in zip(splans, xs, ysp):
+                    sp(xx, yy)
+
+            per_matrix_spmm()
+            pm_spmm_ms = statistics.median(cuda_event_ms(per_matrix_spmm, stream, 5))
+            for sp in splans:
+                sp.close()
+            del splans, ysp
         num = den = 0.0
         for y, ycs in zip(ys, yc):
             yy = y.view(y.shape[0], -1)
@@ -582,6 +624,9 @@ def run_batch_extra(dev, stream, args):
         res[f"k{k}"] = {
             "batched_ms": round(b_ms, 3), "per_matrix_ms": round(p_ms, 3),
             "speedup_vs_per_matrix": round(p_ms / b_ms, 3),
+            "per_matrix_spmm_ms": None if pm_spmm_ms is None else round(pm_spmm_ms, 3),
+            "speedup_vs_per_matrix_spmm": (None if pm_spmm_ms is None
+                                           else round(pm_spmm_ms / b_ms, 3)),
             "gbs": round(bytes_k / b_ms / 1e6, 1), "frac_hbm": round(bytes_k / b_ms / 1e6 / pk, 4),
             "fp64_tflops": round(flops / b_ms / 1e9, 4), "s": s_best,
             "tuner_ms": {str(sv): round(t, 3) for sv, t in s_times.items()},

@@ -279,6 +279,64 @@ int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_val, const i
                              csr_col, work, work_bytes, static_cast<cudaStream_t>(stream));
 }
 
+size_t sblas_cscmv_workspace_bytes(int m, int n, long long nnz)
+{
+    return cscmv_workspace_bytes(m, n, nnz);
+}
+
+int sblas_dcscmv(int m, int n, long long nnz, double alpha, const double *val, const int *colptr,
+                 const int *rowidx, const double *x, double beta, double *y, void *work,
+                 size_t work_bytes, void *stream)
+{
+    clear_error();
+    if (m < 0 || n < 0 || nnz < 0 || nnz > 0x7fffffffLL) {
+        set_error(SBLAS_ERR_ARG, "bad sizes m=%d n=%d nnz=%lld", m, n, nnz);
+        return SBLAS_ERR_ARG;
+    }
+    if (m == 0) return SBLAS_OK;
+    if (y == nullptr || (nnz > 0 && (val == nullptr || colptr == nullptr || rowidx == nullptr ||
+                                     x == nullptr))) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    const size_t need = cscmv_workspace_bytes(m, n, nnz);
+    if (work == nullptr) {
+        work = device_scratch(14, need);
+        work_bytes = need;
+        if (!work) {
+            set_error(SBLAS_ERR_ALLOC, "cannot allocate %zu bytes of workspace", need);
+            return SBLAS_ERR_ALLOC;
+        }
+    }
+    return launch_cscmv(m, n, nnz, alpha, val, colptr, rowidx, x, beta, y, work, work_bytes,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int sblas_csc_analyse(int m, int n, long long nnz, const int *colptr, const int *rowidx,
+                      void *work, size_t work_bytes, void *stream)
+{
+    clear_error();
+    if (nnz > 0 && (colptr == nullptr || rowidx == nullptr)) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_csc_analyse(m, n, nnz, colptr, rowidx, work, work_bytes,
+                              static_cast<cudaStream_t>(stream));
+}
+
+int sblas_dcscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
+                          const double *x, double beta, double *y, void *work, size_t work_bytes,
+                          void *stream)
+{
+    clear_error();
+    if (m > 0 && (y == nullptr || (nnz > 0 && (val == nullptr || x == nullptr)))) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_cscmv_analysed(m, n, nnz, alpha, val, x, beta, y, work, work_bytes,
+                                 static_cast<cudaStream_t>(stream));
+}
+
 size_t sblas_csr_transpose_workspace_bytes(int m, int n, long long nnz)
 {
     return csr_transpose_workspace_bytes(m, n, nnz);

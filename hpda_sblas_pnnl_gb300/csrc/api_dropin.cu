@@ -317,32 +317,8 @@ spmv_ret run_host(Call c)
     const int *rowptr = d_ptr;
     const int *col = d_idx;
     const double *val = d_val;
-    if (c.fmt == Fmt::CSC && nnz > 0) {
-        const size_t wb = csc_to_csr_workspace_bytes(m, n, nnz);
-        void *w = device_scratch(6, wb);
-        const size_t vb = (sizeof(double) * (size_t)nnz + 255) & ~size_t(255);
-        const size_t cb = (sizeof(int) * (size_t)nnz + 255) & ~size_t(255);
-        unsigned char *o = static_cast<unsigned char *>(
-            device_scratch(7, vb + cb + sizeof(int) * (size_t)(m + 1)));
-        if (!w || !o) {
-            set_error(SBLAS_ERR_ALLOC, "%s: device allocation failed", c.name);
-            return failed();
-        }
-        double *o_val = reinterpret_cast<double *>(o);
-        int *o_col = reinterpret_cast<int *>(o + vb);
-        int *o_ptr = reinterpret_cast<int *>(o + vb + cb);
-        if (launch_csc_to_csr(m, n, nnz, d_val, d_ptr, d_idx, o_val, o_ptr, o_col, w, wb, st) !=
-            SBLAS_OK)
-            return failed();
-        rowptr = o_ptr;
-        col = o_col;
-        val = o_val;
-    } else if (c.fmt == Fmt::CSC) {
-        int *o_ptr = static_cast<int *>(device_scratch(7, sizeof(int) * (size_t)(m + 1)));
-        if (!o_ptr || launch_coo_rows_to_rowptr(m, 0, nullptr, o_ptr, st) != SBLAS_OK)
-            return failed();
-        rowptr = o_ptr;
-    } else if (c.fmt == Fmt::COO) {
+    const bool csc_direct = (c.fmt == Fmt::CSC);   // summed by row blocks, no CSR copy
+    if (c.fmt == Fmt::COO) {
         int *o_ptr = static_cast<int *>(device_scratch(7, sizeof(int) * (size_t)(m + 1)));
         if (!o_ptr || launch_coo_rows_to_rowptr(m, nnz, d_ptr, o_ptr, st) != SBLAS_OK)
             return failed();
@@ -354,7 +330,22 @@ spmv_ret run_host(Call c)
     const int rows = c.row_hi - c.row_lo;
     const double beta_eff = c.additive ? c.beta + 1.0 : c.beta;
     void *tile_work = nullptr;   // workspace of the tile launch, if one ran
-    if (rows > 0) {
+    if (csc_direct && rows > 0) {
+        // the CSC product: the row-ordered structure by a stable bucket sort
+        // (inspector), then the values in row order and the tile kernel
+        const size_t wb = cscmv_workspace_bytes(m, n, nnz);
+        void *w = device_scratch(6, wb);
+        if (!w) {
+            set_error(SBLAS_ERR_ALLOC, "%s: workspace allocation failed", c.name);
+            return failed();
+        }
+        if (launch_csc_analyse(m, n, nnz, d_ptr, d_idx, w, wb, st) != SBLAS_OK) return failed();
+        DROPIN_CUDA(cudaEventRecord(e2, st));   // the inspector counts as format work
+        if (launch_cscmv_analysed(m, n, nnz, c.alpha, d_val, d_x, beta_eff, d_y, w, wb, st) !=
+            SBLAS_OK)
+            return failed();
+        if (nnz > 0 && n > 0) tile_work = csc_tile_workspace(w, m, n, nnz);
+    } else if (rows > 0) {
         // a row sub-range keeps absolute offsets into col/val
         const int *rp = rowptr + c.row_lo;
         double *yp = d_y + c.row_lo;
@@ -739,7 +730,8 @@ namespace {
 // sorted triplets go to oval/orow/ocol (may alias the inputs) and, when
 // optr is non-null, the compressed pointer of the sort key (nkeys + 1).
 // Same result as the reference's cuSPARSE coosort + coo2csr
-// (src/spmv_helper.cu:277-387, :493-642).
+// (src/spmv_helper.cu:277-387, :493-642): a stable sort by the key index
+// carrying the other index and the value (this library's bucket passes).
 int host_coo_sort(int m, int n, int nnz, const double *val, const int *row, const int *col,
                   bool by_row, double *oval, int *orow, int *ocol, int *optr)
 {
@@ -760,14 +752,12 @@ int host_coo_sort(int m, int n, int nnz, const double *val, const int *row, cons
     int *d_row = static_cast<int *>(device_scratch(2, sizeof(int) * nb));
     int *d_col = static_cast<int *>(device_scratch(3, sizeof(int) * nb));
     int *d_keys = static_cast<int *>(device_scratch(8, sizeof(int) * nb));
-    int *d_perm = static_cast<int *>(device_scratch(9, sizeof(int) * nb));
-    const size_t wb = sort_perm_workspace_bytes(nkeys, nnz);
+    const size_t wb = coo_sort_workspace_bytes(nkeys, nnz);
     void *d_work = device_scratch(10, wb);
     int *d_other = static_cast<int *>(device_scratch(11, sizeof(int) * nb));
     double *d_oval = static_cast<double *>(device_scratch(12, sizeof(double) * nb));
     int *d_ptr = static_cast<int *>(device_scratch(13, sizeof(int) * (size_t)(nkeys + 1)));
-    if (!d_val || !d_row || !d_col || !d_keys || !d_perm || !d_work || !d_other || !d_oval ||
-        !d_ptr) {
+    if (!d_val || !d_row || !d_col || !d_keys || !d_work || !d_other || !d_oval || !d_ptr) {
         set_error(SBLAS_ERR_ALLOC, "COO sort: device allocation failed");
         return SBLAS_ERR_ALLOC;
     }
@@ -778,8 +768,8 @@ int host_coo_sort(int m, int n, int nnz, const double *val, const int *row, cons
     }
     const int *keys = by_row ? d_row : d_col;
     const int *other = by_row ? d_col : d_row;
-    int rc = launch_sort_perm(nkeys, nnz, keys, d_keys, d_perm, d_work, wb, st);
-    if (rc == SBLAS_OK) rc = launch_gather(nnz, d_perm, other, d_other, d_val, d_oval, st);
+    int rc = launch_coo_sort(nkeys, nnz, keys, other, d_val, d_keys, d_other, d_oval, d_work, wb,
+                             st);
     if (rc == SBLAS_OK && optr) rc = launch_coo_rows_to_rowptr(nkeys, nnz, d_keys, d_ptr, st);
     if (rc != SBLAS_OK) return rc;
     if (nnz > 0) {

@@ -1,23 +1,21 @@
 // Stable bucket scatter by one digit of an int key: the building block of
-// this library's sorts and of the atomic-free CSC SpMV (own kernels; no
-// library sort).
+// this library's sorts (own kernels; no library sort).
 //
-// One pass over n entries, digit d(e) = (key(e) >> shift) & (nb - 1), nb <= 2048:
-//   bucket_hist_kernel   per CTA tile (TILE entries): digit counts (shared-memory
-//                        counters), written bucket-major: table[d * ntiles + t]
-//   exclusive scan       of the table (scan_* kernels): entry (d, t) becomes the
-//                        output position of tile t's first entry of digit d
-//   bucket_scatter_kernel per tile, stable ranks of its entries: every warp walks
-//                        its TILE / NW entries in order, ranking equal digits with
-//                        a warp match and counting in a warp-private shared table;
-//                        a prefix over the warps per digit turns those counts into
-//                        offsets; each entry then goes to
-//                        scanned(d, t) + warp offset + rank, and the Op writes its
-//                        payloads there.
+// One pass over n entries, digit d(e) = (key(e) >> shift) & (nb - 1), nb <= 256:
+//   bucket_hist_kernel    per CTA tile (TILE entries): digit counts (shared-
+//                         memory counters), written digit-major: table[d * ntiles + t]
+//   exclusive scan        of the table (scan_* kernels): entry (d, t) becomes the
+//                         output position of tile t's first entry of digit d
+//   bucket_scatter_kernel per tile: stable ranks of its entries (every warp walks
+//                         its TILE / NW entries in order, ranking equal digits with
+//                         a warp match and counting in a warp-private shared
+//                         table), the tile sorted by digit in shared memory with
+//                         its payloads, then written out so that consecutive
+//                         threads write consecutive positions of one digit's run
+//                         (about TILE / nb entries): coalesced stores.
 // Entries keep their input order inside every digit (tiles in order, warps in
 // order inside a tile, entries in order inside a warp): a least-significant-
-// digit sequence of passes is a stable sort, and a single pass on the high
-// bits groups entries into buckets in input order.  Counts are integers and
+// digit sequence of passes is a stable sort.  Counts are integers and
 // positions are computed, not claimed with atomics: every run produces the
 // same output.
 #pragma once
@@ -28,13 +26,16 @@
 
 namespace sblas {
 namespace bsort {
+// internal linkage: every translation unit that includes this header gets its
+// own copy of the kernels (no relocatable device code)
+namespace {
 
 constexpr int NW = 8;                   // warps per CTA
 constexpr int THREADS = NW * 32;
-constexpr int ITER = 64;                // entries per lane per tile
-constexpr int WSPAN = 32 * ITER;        // entries of one warp in a tile (2048)
-constexpr int TILE = NW * WSPAN;        // entries per CTA tile (16384)
-constexpr int MAXB = 2048;              // digit values per pass
+constexpr int ITER = 16;                // entries per lane per tile
+constexpr int WSPAN = 32 * ITER;        // entries of one warp in a tile (512)
+constexpr int TILE = NW * WSPAN;        // entries per CTA tile (4096)
+constexpr int MAXB = 256;               // digit values per pass (8-bit digits)
 
 __host__ __device__ inline long long num_tiles(long long n) { return (n + TILE - 1) / TILE; }
 
@@ -199,38 +200,58 @@ inline int exclusive_scan(const int *in, int *out, long long n, void *tmp, int *
 }
 
 // ---- pass 2: stable scatter ------------------------------------------------
+// What an entry carries besides its key: up to two ints and one double.
+struct Payload {
+    int a;
+    int b;
+    double d;
+};
+
 // Op: __device__ int key(long long e) const: the sort key of entry e;
-//     __device__ void emit(State &st, long long e0, int lane, bool valid,
-//                          long long e, int key, long long pos) const:
-//     called by all 32 lanes of a warp for the 32 consecutive entries
-//     e0 .. e0 + 31 (in increasing e0 per warp, so Op::State may carry a
-//     cursor); writes entry e's outputs at position pos when valid.
+//     __device__ Payload load(State &st, long long e0, int lane, bool valid,
+//                             long long e) const: entry e's payload, called by
+//     all 32 lanes of a warp for the 32 consecutive entries e0 .. e0 + 31 (in
+//     increasing e0 per warp, so Op::State may carry a cursor);
+//     members key_out, a_out, b_out, d_out: the pass's outputs (a, b, d may
+//     be null: not carried).
 template <class Op>
-__global__ void __launch_bounds__(THREADS) bucket_scatter_kernel(const Op op, long long n,
+__global__ void __launch_bounds__(THREADS, 2) bucket_scatter_kernel(const Op op, long long n,
                                                                  int shift, int nb, int ntiles,
                                                                  const int *__restrict__ table)
 {
     extern __shared__ __align__(16) unsigned char bs_smem[];
-    // wcnt[w][d]: counts, then each warp's offset inside the tile's run of d
-    unsigned short *wcnt = reinterpret_cast<unsigned short *>(bs_smem);
-    int *gbase = reinterpret_cast<int *>(bs_smem + sizeof(unsigned short) * NW * MAXB);
-    unsigned short *loc = reinterpret_cast<unsigned short *>(
-        bs_smem + sizeof(unsigned short) * NW * MAXB + sizeof(int) * MAXB);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double *st_d = reinterpret_cast<double *>(bs_smem);                  // [TILE]
+    int *st_key = reinterpret_cast<int *>(st_d + TILE);                  // [TILE]
+    int *st_a = st_key + TILE;                                           // [TILE]
+    int *st_b = st_a + TILE;                                             // [TILE]
+    unsigned short *loc = reinterpret_cast<unsigned short *>(st_b + TILE);   // [TILE]
+    unsigned short *wcnt = loc + TILE;                                   // [NW][MAXB]
+    int *gbase = reinterpret_cast<int *>(wcnt + NW * MAXB);              // [MAXB]
+    int *toff = gbase + MAXB;                                            // [MAXB]
+    __shared__ int wtot[NW];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long t0 = (long long)blockIdx.x * TILE;
     const long long wbeg = t0 + (long long)w * WSPAN;
-    for (int i = threadIdx.x; i < NW * nb; i += THREADS) wcnt[(i / nb) * MAXB + (i % nb)] = 0;
-    for (int d = threadIdx.x; d < nb; d += THREADS)
+    const int cnt = (int)min((long long)TILE, n - t0);
+    for (int i = tid; i < NW * MAXB; i += THREADS) wcnt[i] = 0;
+    for (int d = tid; d < nb; d += THREADS)
         gbase[d] = __ldg(table + (long long)d * ntiles + blockIdx.x);
+    // this warp's keys, all loads in flight at once
+    int kr[ITER];
+#pragma unroll
+    for (int i = 0; i < ITER; ++i) {
+        const long long e = wbeg + (long long)i * 32 + lane;
+        kr[i] = e < n ? op.key(e) : 0;
+    }
     __syncthreads();
     unsigned short *mycnt = wcnt + w * MAXB;
     const unsigned lt = (1u << lane) - 1u;
     // ranks: entries of this warp in order (batch i, then lane)
+#pragma unroll
     for (int i = 0; i < ITER; ++i) {
         const long long e = wbeg + (long long)i * 32 + lane;
-        if (wbeg + (long long)i * 32 >= n) break;                  // warp-uniform
         const bool valid = e < n;
-        const int d = valid ? digit_of(op.key(e), shift, nb) : -1 - lane;   // invalid: unique
+        const int d = valid ? digit_of(kr[i], shift, nb) : -1 - lane;   // invalid: unique
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int base = valid ? (int)mycnt[d] : 0;
         __syncwarp();
@@ -241,38 +262,68 @@ __global__ void __launch_bounds__(THREADS) bucket_scatter_kernel(const Op op, lo
         __syncwarp();
     }
     __syncthreads();
-    // per digit: warps' counts -> their offsets inside the tile's run
-    for (int d = threadIdx.x; d < nb; d += THREADS) {
-        int run = 0;
+    // per digit: the warps' offsets inside the digit's run, the run lengths
+    int total = 0;
+    if (tid < nb) {
 #pragma unroll
         for (int k = 0; k < NW; ++k) {
-            const int c = wcnt[k * MAXB + d];
-            wcnt[k * MAXB + d] = (unsigned short)run;
-            run += c;
+            const int c = wcnt[k * MAXB + tid];
+            wcnt[k * MAXB + tid] = (unsigned short)total;
+            total += c;
+        }
+    }
+    // exclusive scan of the run lengths over the digits: each run's start in
+    // the tile's sorted order (nb <= THREADS: one digit per thread)
+    int v = total;
+#pragma unroll
+    for (int k = 1; k < 32; k <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, v, k);
+        if (lane >= k) v += o;
+    }
+    if (lane == 31) wtot[w] = v;
+    __syncthreads();
+    int before = 0;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) before += (k < w) ? wtot[k] : 0;
+    if (tid < nb) toff[tid] = before + v - total;
+    __syncthreads();
+    // the tile in digit order, with its payloads, in shared memory
+    typename Op::State st{};
+    const bool ha = op.a_out != nullptr, hb = op.b_out != nullptr, hd = op.d_out != nullptr;
+#pragma unroll
+    for (int i = 0; i < ITER; ++i) {
+        const long long e0 = wbeg + (long long)i * 32;
+        if (e0 < n) {                                              // warp-uniform
+            const long long e = e0 + lane;
+            const bool valid = e < n;
+            const Payload pl = op.load(st, e0, lane, valid, e);
+            if (valid) {
+                const int d = digit_of(kr[i], shift, nb);
+                const int slot = toff[d] + mycnt[d] + loc[w * WSPAN + i * 32 + lane];
+                st_key[slot] = kr[i];
+                if (ha) st_a[slot] = pl.a;
+                if (hb) st_b[slot] = pl.b;
+                if (hd) st_d[slot] = pl.d;
+            }
         }
     }
     __syncthreads();
-    typename Op::State st{};
-    for (int i = 0; i < ITER; ++i) {
-        const long long e0 = wbeg + (long long)i * 32;
-        if (e0 >= n) break;                                        // warp-uniform
-        const long long e = e0 + lane;
-        const bool valid = e < n;
-        int key = 0;
-        long long pos = 0;
-        if (valid) {
-            key = op.key(e);
-            const int d = digit_of(key, shift, nb);
-            pos = (long long)gbase[d] + mycnt[d] + loc[w * WSPAN + i * 32 + lane];
-        }
-        op.emit(st, e0, lane, valid, e, key, pos);
+    // write-out: consecutive slots of one digit go to consecutive positions
+    for (int j = tid; j < cnt; j += THREADS) {
+        const int k = st_key[j];
+        const int d = digit_of(k, shift, nb);
+        const long long pos = (long long)gbase[d] + (j - toff[d]);
+        if (op.key_out) op.key_out[pos] = k;
+        if (ha) op.a_out[pos] = st_a[j];
+        if (hb) op.b_out[pos] = st_b[j];
+        if (hd) op.d_out[pos] = st_d[j];
     }
 }
 
 inline size_t scatter_smem_bytes()
 {
-    return sizeof(unsigned short) * NW * MAXB + sizeof(int) * MAXB +
-           sizeof(unsigned short) * TILE;
+    return (sizeof(double) + 3 * sizeof(int) + sizeof(unsigned short)) * TILE +
+           sizeof(unsigned short) * NW * MAXB + 2 * sizeof(int) * MAXB;
 }
 
 // Table bytes (counts / positions) and scan scratch of one pass over n entries.
@@ -287,12 +338,9 @@ inline size_t pass_work_bytes(long long n, int nb)
 }
 
 // One stable pass: entries of `op` scattered by digit (key >> shift) & (nb-1).
-// work: pass_work_bytes(n, nb) bytes; on return the table holds, at
-// [d * ntiles], the start of digit d's run for every d (and the runs end at
-// n), stream-ordered.
+// work: pass_work_bytes(n, nb) bytes.  Stream-ordered.
 template <class Op>
-int scatter_pass(const Op &op, long long n, int shift, int nb, void *work, cudaStream_t stream,
-                 int **table_out = nullptr)
+int scatter_pass(const Op &op, long long n, int shift, int nb, void *work, cudaStream_t stream)
 {
     if (n <= 0) return SBLAS_OK;
     if (nb < 1 || nb > MAXB || (nb & (nb - 1)) != 0) {
@@ -317,9 +365,123 @@ int scatter_pass(const Op &op, long long n, int shift, int nb, void *work, cudaS
                                         (int)smem));
     kfn<<<(unsigned)nt, THREADS, smem, stream>>>(op, n, shift, nb, (int)nt, table);
     SBLAS_CUDA_TRY(cudaGetLastError());
-    if (table_out) *table_out = table;
     return SBLAS_OK;
 }
 
+// ---- segment of an entry in a compressed pointer array --------------------
+// ptr[0..nseg] (ptr[0] = 0, ptr[nseg] = entries, nondecreasing): the segment
+// (column of CSC, row of CSR) of entry e is the largest s with ptr[s] <= e.
+// A warp walking increasing batches e0 .. e0 + 31 keeps the segment of its
+// last batch in `cur` (-1 before the first): every batch then loads the 32
+// segment starts after it (coalesced) and each lane counts those <= its
+// entry with a 5-step shuffle search; runs of more than 32 short or empty
+// segments take further rounds.
+struct SegCursor {
+    int cur = -1;
+};
+
+__device__ __forceinline__ int segment_of(const int *__restrict__ ptr, int nseg, SegCursor &c,
+                                          long long e0, int lane, bool valid, long long e)
+{
+    if (c.cur < 0) {
+        int lo = 0, hi = nseg - 1;   // largest s with ptr[s] <= e0 (warp-uniform)
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((long long)__ldg(ptr + mid) <= e0) lo = mid; else hi = mid - 1;
+        }
+        c.cur = lo;
+    }
+    const int ev = valid ? (int)e : INT_MIN;   // invalid lanes are found at once
+    int base = c.cur, seg = c.cur;
+    bool found = !valid;
+    for (;;) {
+        const int idx = base + 1 + lane;
+        const int st = idx <= nseg ? __ldg(ptr + idx) : INT_MAX;
+        int pos = 0;   // number of the 32 starts <= ev
+#pragma unroll
+        for (int b = 16; b > 0; b >>= 1) {
+            const int v = __shfl_sync(0xffffffffu, st, pos + b - 1);
+            if (v <= ev) pos += b;
+        }
+        const int v31 = __shfl_sync(0xffffffffu, st, 31);
+        if (pos == 31 && v31 <= ev) pos = 32;
+        if (!found && pos < 32) {
+            seg = base + pos;
+            found = true;
+        }
+        if (__all_sync(0xffffffffu, found)) break;
+        base += 32;
+    }
+    c.cur = __shfl_sync(0xffffffffu, valid ? seg : c.cur, 31);
+    return seg < nseg ? seg : nseg - 1;   // a malformed pointer never indexes past it
+}
+
+// ---- operations of the sorts ------------------------------------------------
+// Moves (key, a, b, d) from arrays to the pass's output positions; any of
+// a, b, d may be absent (null input and output).
+struct MoveOp {
+    const int *key_in;
+    const int *a_in;
+    const int *b_in;
+    const double *d_in;
+    int *key_out;
+    int *a_out;
+    int *b_out;
+    double *d_out;
+    struct State {};
+    __device__ int key(long long e) const { return __ldg(key_in + e); }
+    __device__ Payload load(State &, long long, int, bool valid, long long e) const
+    {
+        Payload p{0, 0, 0.0};
+        if (valid) {
+            if (a_in) p.a = __ldg(a_in + e);
+            if (b_in) p.b = __ldg(b_in + e);
+            if (d_in) p.d = __ldg(d_in + e);
+        }
+        return p;
+    }
+};
+
+// A compressed matrix's entries keyed by their index array (CSC: the row of
+// every entry), carrying the segment each entry belongs to (CSC: its column)
+// as `a`, the entry's own position as `b` and its value as `d`, as the
+// outputs ask.
+struct SegmentOp {
+    const int *key_in;
+    const int *ptr;      // segment pointer, nseg + 1 entries
+    int nseg;
+    const double *d_in;  // values, or null
+    int *key_out;
+    int *a_out;          // segment of the entry, or null
+    int *b_out;          // position of the entry, or null
+    double *d_out;
+    struct State {
+        SegCursor c;
+    };
+    __device__ int key(long long e) const { return __ldg(key_in + e); }
+    __device__ Payload load(State &st, long long e0, int lane, bool valid, long long e) const
+    {
+        Payload p{0, (int)e, 0.0};
+        if (a_out) p.a = segment_of(ptr, nseg, st.c, e0, lane, valid, e);
+        if (valid && d_in) p.d = __ldg(d_in + e);
+        return p;
+    }
+};
+
+// Digit widths of a least-significant-digit sort of keys in [0, key_bound):
+// as few passes as digits of at most 8 bits allow, equal widths.
+struct LsdPlan {
+    int passes;
+    int width;
+};
+inline LsdPlan lsd_plan(long long key_bound)
+{
+    int bits = 1;
+    while (bits < 31 && (1LL << bits) < key_bound) ++bits;
+    const int passes = (bits + 7) / 8;
+    return LsdPlan{passes, (bits + passes - 1) / passes};
+}
+
+}  // namespace
 }  // namespace bsort
 }  // namespace sblas

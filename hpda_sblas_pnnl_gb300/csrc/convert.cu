@@ -3,19 +3,23 @@
 // The reference converts on the GPU with cuSPARSE: coo2csrGPU =
 // cusparseXcoo2csr (src/spmv_helper.cu:478-490) after a stable row sort
 // (sortCOORowGPU, :427-443); coo2csc = a stable column sort then the same
-// compression with rows and columns swapped (:575-642).  Here:
+// compression with rows and columns swapped (:575-642).  Here, with this
+// library's own kernels only:
 //   * row-sorted COO -> CSR row pointer: atomic-free boundary detection (each
 //     nonzero whose row differs from its left neighbour writes the row
 //     pointer entries of the rows in between);
-//   * CSC -> CSR: a stable radix sort of (row, CSC position) pairs (CUB,
-//     part of the CUDA toolkit), then a gather of column and value; stability
-//     keeps columns ascending inside each row, as cuSPARSE's stable coosort;
+//   * sorts (CSC -> CSR, A -> A^T, the COO sorts): a stable least-significant-
+//     digit sort by the row (or column) index, digits of at most 11 bits
+//     (bucket_sort.cuh: per-tile digit counts, an exclusive scan, a stable
+//     scatter): two passes for keys below 4M, three up to 2^31.  The first
+//     pass derives what the entries carry from the source (a CSC entry's
+//     column from the column pointer, an entry's own position), so no
+//     permutation has to be applied afterwards; stability keeps the second
+//     index ascending inside each row, as cuSPARSE's stable coosort does;
 //   * spMspV's x-zero filter: a keep flag per nonzero, an exclusive scan of
-//     the flags (CUB) giving every kept nonzero its output position and every
-//     row its new row pointer, then a scatter.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
-
+//     the flags giving every kept nonzero its output position and every row
+//     its new row pointer, then a scatter.
+#include "bucket_sort.cuh"
 #include "sblas_internal.h"
 
 namespace sblas {
@@ -87,44 +91,11 @@ __global__ void zero_rowptr_kernel(int m, int *rowptr)
         rowptr[i] = 0;
 }
 
-__global__ void iota_kernel(long long nnz, int *v)
-{
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
-         k += (long long)gridDim.x * blockDim.x)
-        v[k] = (int)k;
-}
-
-// CSC position k -> its column (largest j with colptr[j] <= k, skipping
-// empty columns), then gather column and value into CSR order.
-__global__ void csc_gather_kernel(int n, long long nnz, const int *__restrict__ colptr,
-                                  const int *__restrict__ perm, const double *__restrict__ cval,
-                                  int *__restrict__ ocol, double *__restrict__ oval)
-{
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int k = __ldg(perm + p);
-        int lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(colptr + mid) <= k) lo = mid; else hi = mid - 1;
-        }
-        ocol[p] = lo;
-        oval[p] = __ldg(cval + k);
-    }
-}
-
 int grid_for(long long items, int threads)
 {
     const long long want = (items + threads - 1) / threads;
     const long long cap = 8LL * device_num_sms();
     return (int)(want < 1 ? 1 : (want < cap ? want : cap));
-}
-
-int end_bit_for(int m)
-{
-    int b = 1;
-    while (b < 31 && (1LL << b) < (long long)m) ++b;
-    return b;
 }
 
 size_t al256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -150,14 +121,99 @@ int launch_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *row
     return SBLAS_OK;
 }
 
+namespace {
+
+// Buffers of one stable least-significant-digit sort of n entries: the pass
+// scratch (digit-count table, scan sums) and, for two passes or more, one or
+// two sets of intermediate arrays (key, a, b, d as present).
+struct LsdLayout {
+    size_t pass = 0, set = 0, total = 0;
+    int passes = 0, width = 0;
+};
+
+LsdLayout lsd_layout(long long n, long long key_bound, bool has_a, bool has_b, bool has_d)
+{
+    LsdLayout L;
+    const bsort::LsdPlan plan = bsort::lsd_plan(key_bound);
+    L.passes = plan.passes;
+    L.width = plan.width;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    L.pass = al256(bsort::pass_work_bytes(n > 0 ? n : 1, 1 << plan.width));
+    L.set = al256(4 * nn) + (has_a ? al256(4 * nn) : 0) + (has_b ? al256(4 * nn) : 0) +
+            (has_d ? al256(8 * nn) : 0);
+    L.total = L.pass + (size_t)(L.passes >= 3 ? 2 : (L.passes == 2 ? 1 : 0)) * L.set;
+    return L;
+}
+
+struct ArraySet {
+    int *key = nullptr, *a = nullptr, *b = nullptr;
+    double *d = nullptr;
+};
+
+ArraySet array_set(unsigned char *p, long long n, bool has_a, bool has_b, bool has_d)
+{
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    ArraySet s;
+    s.key = reinterpret_cast<int *>(p);
+    p += al256(4 * nn);
+    if (has_a) {
+        s.a = reinterpret_cast<int *>(p);
+        p += al256(4 * nn);
+    }
+    if (has_b) {
+        s.b = reinterpret_cast<int *>(p);
+        p += al256(4 * nn);
+    }
+    if (has_d) s.d = reinterpret_cast<double *>(p);
+    return s;
+}
+
+// Stable sort of n entries by key in [0, key_bound).  Pass 1 reads through
+// `first` (its outputs are set here); later passes move the arrays; the last
+// pass writes `out` (out.key required; out.a / out.b / out.d as the first
+// operation carries them).
+template <class FirstOp>
+int lsd_sort(FirstOp first, long long n, long long key_bound, const ArraySet &out, void *work,
+             size_t work_bytes, cudaStream_t stream)
+{
+    if (n <= 0) return SBLAS_OK;
+    const bool has_a = out.a != nullptr, has_b = out.b != nullptr, has_d = out.d != nullptr;
+    const LsdLayout L = lsd_layout(n, key_bound, has_a, has_b, has_d);
+    if (work == nullptr || work_bytes < L.total) {
+        set_error(SBLAS_ERR_ARG, "sort workspace too small (%zu < %zu)", work_bytes, L.total);
+        return SBLAS_ERR_ARG;
+    }
+    unsigned char *w = static_cast<unsigned char *>(work);
+    ArraySet tmp[2] = {array_set(w + L.pass, n, has_a, has_b, has_d),
+                       array_set(w + L.pass + L.set, n, has_a, has_b, has_d)};
+    const int nb = 1 << L.width;
+    for (int p = 0; p < L.passes; ++p) {
+        const ArraySet &dst = (p == L.passes - 1) ? out : tmp[p % 2];
+        int rc;
+        if (p == 0) {
+            FirstOp op = first;
+            op.key_out = dst.key;
+            op.a_out = dst.a;
+            op.b_out = dst.b;
+            op.d_out = dst.d;
+            rc = bsort::scatter_pass(op, n, 0, nb, w, stream);
+        } else {
+            const ArraySet &src = tmp[(p - 1) % 2];
+            bsort::MoveOp op{src.key, src.a, src.b, src.d, dst.key, dst.a, dst.b, dst.d};
+            rc = bsort::scatter_pass(op, n, p * L.width, nb, w, stream);
+        }
+        if (rc != SBLAS_OK) return rc;
+    }
+    return SBLAS_OK;
+}
+
+}  // namespace
+
 size_t csc_to_csr_workspace_bytes(int m, int n, long long nnz)
 {
     (void)n;
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(m));
-    return al256(cub_bytes) + 3 * al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+    const size_t nn = (size_t)(nnz > 0 ? nnz : 1);
+    return al256(4 * nn) + lsd_layout(nnz, m, true, false, true).total;
 }
 
 int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val, const int *csc_colptr,
@@ -169,62 +225,41 @@ int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val, const 
         return SBLAS_ERR_ARG;
     }
     if (nnz == 0) return launch_coo_rows_to_rowptr(m, 0, nullptr, csr_rowptr, stream);
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(m));
-    const size_t need = al256(cub_bytes) + 3 * al256(sizeof(int) * (size_t)nnz);
+    const size_t need = csc_to_csr_workspace_bytes(m, n, nnz);
     if (work == nullptr || work_bytes < need) {
         set_error(SBLAS_ERR_ARG, "csc_to_csr workspace too small (%zu < %zu)", work_bytes, need);
         return SBLAS_ERR_ARG;
     }
     unsigned char *w = static_cast<unsigned char *>(work);
-    void *cub_tmp = w;
-    int *perm_in = reinterpret_cast<int *>(w + al256(cub_bytes));
-    int *perm_out = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * nnz));
-    int *rows_sorted =
-        reinterpret_cast<int *>(w + al256(cub_bytes) + 2 * al256(sizeof(int) * nnz));
-    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, perm_in);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(cub_tmp, cub_bytes, csc_row,
-                                                              rows_sorted, perm_in, perm_out,
-                                                              (int)nnz, 0, end_bit_for(m),
-                                                              stream)));
-    csc_gather_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(n, nnz, csc_colptr, perm_out,
-                                                              csc_val, csr_col, csr_val);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    return launch_coo_rows_to_rowptr(m, nnz, rows_sorted, csr_rowptr, stream);
+    ArraySet out;
+    out.key = reinterpret_cast<int *>(w);   // the rows, sorted: the row pointer's source
+    out.a = csr_col;
+    out.d = csr_val;
+    // pass 1 reads the CSC arrays: key = row, a = column (from the column
+    // pointer), d = value
+    bsort::SegmentOp first{csc_row, csc_colptr, n, csc_val, nullptr, nullptr, nullptr, nullptr};
+    const int rc = lsd_sort(first, nnz, m, out, w + al256(4 * (size_t)nnz),
+                            work_bytes - al256(4 * (size_t)nnz), stream);
+    if (rc != SBLAS_OK) return rc;
+    return launch_coo_rows_to_rowptr(m, nnz, out.key, csr_rowptr, stream);
 }
 
-size_t sort_perm_workspace_bytes(int key_bound, long long nnz)
+size_t coo_sort_workspace_bytes(int key_bound, long long nnz)
 {
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(key_bound));
-    return al256(cub_bytes) + al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+    return lsd_layout(nnz, key_bound, true, false, true).total;
 }
 
-int launch_sort_perm(int key_bound, long long nnz, const int *keys, int *keys_sorted, int *perm,
-                     void *work, size_t work_bytes, cudaStream_t stream)
+int launch_coo_sort(int key_bound, long long nnz, const int *keys, const int *other,
+                    const double *val, int *keys_out, int *other_out, double *val_out,
+                    void *work, size_t work_bytes, cudaStream_t stream)
 {
     if (nnz <= 0) return SBLAS_OK;
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(key_bound));
-    if (work_bytes < al256(cub_bytes) + al256(sizeof(int) * (size_t)nnz)) {
-        set_error(SBLAS_ERR_ARG, "sort workspace too small");
-        return SBLAS_ERR_ARG;
-    }
-    unsigned char *w = static_cast<unsigned char *>(work);
-    int *iota = reinterpret_cast<int *>(w + al256(cub_bytes));
-    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, iota);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(w, cub_bytes, keys, keys_sorted, iota,
-                                                              perm, (int)nnz, 0,
-                                                              end_bit_for(key_bound), stream)));
-    return SBLAS_OK;
+    ArraySet out;
+    out.key = keys_out;
+    out.a = other_out;
+    out.d = val_out;
+    bsort::MoveOp first{keys, other, nullptr, val, nullptr, nullptr, nullptr, nullptr};
+    return lsd_sort(first, nnz, key_bound, out, work, work_bytes, stream);
 }
 
 namespace {
@@ -242,23 +277,6 @@ __global__ void gather_kernel(long long nnz, const int *__restrict__ perm,
 }  // namespace
 
 namespace {
-// Entry q of A^T is entry perm[q] of A: its column in A^T is the row of A
-// holding position perm[q] (largest r with rowptr[r] <= perm[q]).
-__global__ void transpose_rows_kernel(int m, long long nnz, const int *__restrict__ rowptr,
-                                      const int *__restrict__ perm, int *__restrict__ t_col)
-{
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nnz;
-         q += (long long)gridDim.x * blockDim.x) {
-        const int p = __ldg(perm + q);
-        int lo = 0, hi = m - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(rowptr + mid) <= p) lo = mid; else hi = mid - 1;
-        }
-        t_col[q] = lo;
-    }
-}
-
 __global__ void gather_f32_kernel(long long nnz, const int *__restrict__ perm,
                                   const float *__restrict__ in, float *__restrict__ out)
 {
@@ -271,11 +289,8 @@ __global__ void gather_f32_kernel(long long nnz, const int *__restrict__ perm,
 size_t csr_transpose_workspace_bytes(int m, int n, long long nnz)
 {
     (void)m;
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(n));
-    return al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+    const size_t nn = (size_t)(nnz > 0 ? nnz : 1);
+    return al256(4 * nn) + lsd_layout(nnz, n, true, true, false).total;
 }
 
 int launch_csr_transpose(int m, int n, long long nnz, const int *rowptr, const int *col,
@@ -287,27 +302,22 @@ int launch_csr_transpose(int m, int n, long long nnz, const int *rowptr, const i
         return SBLAS_ERR_ARG;
     }
     if (nnz == 0) return launch_coo_rows_to_rowptr(n, 0, nullptr, t_rowptr, stream);
-    size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs<int, int>(nullptr, cub_bytes, (const int *)nullptr,
-                                              (int *)nullptr, (const int *)nullptr,
-                                              (int *)nullptr, (int)nnz, 0, end_bit_for(n));
-    const size_t need = al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)nnz);
+    const size_t need = csr_transpose_workspace_bytes(m, n, nnz);
     if (work == nullptr || work_bytes < need) {
         set_error(SBLAS_ERR_ARG, "csr_transpose workspace too small (%zu < %zu)", work_bytes, need);
         return SBLAS_ERR_ARG;
     }
     unsigned char *w = static_cast<unsigned char *>(work);
-    int *iota = reinterpret_cast<int *>(w + al256(cub_bytes));
-    int *cols_sorted = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * nnz));
-    iota_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, iota);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    // stable sort by column: entries of one column keep their row order
-    SBLAS_CUDA_TRY((cub::DeviceRadixSort::SortPairs<int, int>(w, cub_bytes, col, cols_sorted, iota,
-                                                              perm, (int)nnz, 0, end_bit_for(n),
-                                                              stream)));
-    transpose_rows_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(m, nnz, rowptr, perm, t_col);
-    SBLAS_CUDA_TRY(cudaGetLastError());
-    return launch_coo_rows_to_rowptr(n, nnz, cols_sorted, t_rowptr, stream);
+    ArraySet out;
+    out.key = reinterpret_cast<int *>(w);   // the columns, sorted: A^T's row pointer source
+    out.a = t_col;                          // the row of A holding the entry
+    out.b = perm;                           // the entry's position in A
+    // stable by column: the entries of one column keep their row order
+    bsort::SegmentOp first{col, rowptr, m, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const int rc = lsd_sort(first, nnz, n, out, w + al256(4 * (size_t)nnz),
+                            work_bytes - al256(4 * (size_t)nnz), stream);
+    if (rc != SBLAS_OK) return rc;
+    return launch_coo_rows_to_rowptr(n, nnz, out.key, t_rowptr, stream);
 }
 
 int launch_gather_values(long long nnz, int val_kind, const void *src, const int *perm, void *dst,
@@ -368,19 +378,13 @@ __global__ void filter_rowptr_kernel(int m, const int *__restrict__ rowptr,
         orowptr[i] = pos[__ldg(rowptr + i)];
 }
 
-size_t filter_cub_bytes(long long nnz)
-{
-    size_t cub_bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (const int *)nullptr, (int *)nullptr,
-                                  (int)(nnz + 1));
-    return cub_bytes;
-}
+size_t filter_scan_bytes(long long nnz) { return bsort::scan_tmp_bytes(nnz + 1); }
 }  // namespace
 
 size_t csr_filter_x_workspace_bytes(long long nnz)
 {
     if (nnz < 0) nnz = 0;
-    return al256(filter_cub_bytes(nnz)) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
+    return al256(filter_scan_bytes(nnz)) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
 }
 
 int launch_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
@@ -391,19 +395,19 @@ int launch_csr_filter_x(int m, long long nnz, const int *rowptr, const int *col,
         set_error(SBLAS_ERR_ARG, "bad sizes m=%d nnz=%lld", m, nnz);
         return SBLAS_ERR_ARG;
     }
-    const size_t cub_bytes = filter_cub_bytes(nnz);
-    const size_t need = al256(cub_bytes) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
+    const size_t scan_bytes = filter_scan_bytes(nnz);
+    const size_t need = al256(scan_bytes) + 2 * al256(sizeof(int) * (size_t)(nnz + 1));
     if (work == nullptr || work_bytes < need) {
         set_error(SBLAS_ERR_ARG, "csr_filter_x workspace too small (%zu < %zu)", work_bytes, need);
         return SBLAS_ERR_ARG;
     }
     unsigned char *w = static_cast<unsigned char *>(work);
-    int *flag = reinterpret_cast<int *>(w + al256(cub_bytes));
-    int *pos = reinterpret_cast<int *>(w + al256(cub_bytes) + al256(sizeof(int) * (nnz + 1)));
+    int *flag = reinterpret_cast<int *>(w + al256(scan_bytes));
+    int *pos = reinterpret_cast<int *>(w + al256(scan_bytes) + al256(sizeof(int) * (nnz + 1)));
     filter_flags_kernel<<<grid_for(nnz + 1, 256), 256, 0, stream>>>(nnz, col, x, flag);
     SBLAS_CUDA_TRY(cudaGetLastError());
-    size_t cb = cub_bytes;
-    SBLAS_CUDA_TRY(cub::DeviceScan::ExclusiveSum(w, cb, flag, pos, (int)(nnz + 1), stream));
+    const int src = bsort::exclusive_scan(flag, pos, nnz + 1, w, nullptr, stream);
+    if (src != SBLAS_OK) return src;
     if (nnz > 0) {
         filter_scatter_kernel<<<grid_for(nnz, 256), 256, 0, stream>>>(nnz, col, val, flag, pos,
                                                                       ocol, oval);

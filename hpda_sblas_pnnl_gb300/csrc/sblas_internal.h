@@ -66,6 +66,30 @@ int tile_workspace_status(void *work, int *out);
 int tile_sticky_status(cudaStream_t stream, bool clear, int *out);
 // Bounded-wait limit of the tile kernels (0 = the default, 2 s) and the
 // test hook that keeps the producer warp from staging (waits then run out).
+// The tile kernel over several matrices in one launch (the batched form
+// with one right-hand side): global tiles [0, ntiles), matrix i owning
+// tiles [tile0s[i], tile0s[i+1]) and partition entries part[part_off_i ..
+// part_off_i + its tiles]; every matrix has at least one tile.  mats: device
+// array of descriptors written by fill_multi_mat.
+struct MultiTileLaunch {
+    const void *mats;
+    const int *tile0s;   // [nmat + 1]
+    int nmat;
+    int ntiles;
+    const int *part;
+    double *carry;       // [ntiles]
+    int *status;
+};
+int multi_tile_sigma();
+size_t multi_tile_count(long long nnz);   // tiles of one matrix (1 when nnz == 0)
+size_t multi_mat_bytes();
+void fill_multi_mat(void *dst, const void *val, const int *rowptr, const int *col,
+                    const double *x, double *y, long long nnz, int m, int tile0, int part_off,
+                    double alpha, double beta, int val_kind);
+int launch_multi_tile_spmv(const MultiTileLaunch &L, int val_kind, cudaStream_t stream);
+// The tile partition of one matrix into part[0 .. ntiles] (nnz > 0).
+int launch_tile_partition(int m, long long nnz, const int *rowptr, int sigma, int *part,
+                          cudaStream_t stream);
 // Configures (under lazy module loading: loads) every kernel of an FP64
 // tile SpMV of shape sigma on the current device.
 int tile_preload_f64(int sigma);
@@ -105,11 +129,28 @@ int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
                       int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,
                       cudaStream_t stream);
 
-// Stable sort of int keys in [0, key_bound) carrying their positions:
-// keys_sorted[p] = keys[perm[p]].  Workspace: sort_perm_workspace_bytes.
-size_t sort_perm_workspace_bytes(int key_bound, long long nnz);
-int launch_sort_perm(int key_bound, long long nnz, const int *keys, int *keys_sorted, int *perm,
-                     void *work, size_t work_bytes, cudaStream_t stream);
+// y = alpha*A*x + beta*y with A in CSC (atomic-free, deterministic):
+// inspector (row-ordered structure + permutation + tile partition into
+// `work`) and executor (value gather + tile kernel).  work:
+// cscmv_workspace_bytes, 256-byte aligned; csc_tile_workspace: the tile
+// workspace inside it (its status word).
+size_t cscmv_workspace_bytes(int m, int n, long long nnz);
+int launch_csc_analyse(int m, int n, long long nnz, const int *colptr, const int *rowidx,
+                       void *work, size_t work_bytes, cudaStream_t stream);
+int launch_cscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
+                          const double *x, double beta, double *y, void *work,
+                          size_t work_bytes, cudaStream_t stream);
+int launch_cscmv(int m, int n, long long nnz, double alpha, const double *val,
+                 const int *colptr, const int *rowidx, const double *x, double beta, double *y,
+                 void *work, size_t work_bytes, cudaStream_t stream);
+void *csc_tile_workspace(void *work, int m, int n, long long nnz);
+// Stable sort of COO entries by keys in [0, key_bound), carrying the other
+// index and the value (bucket_sort.cuh passes).  Workspace:
+// coo_sort_workspace_bytes.
+size_t coo_sort_workspace_bytes(int key_bound, long long nnz);
+int launch_coo_sort(int key_bound, long long nnz, const int *keys, const int *other,
+                    const double *val, int *keys_out, int *other_out, double *val_out,
+                    void *work, size_t work_bytes, cudaStream_t stream);
 // out_i[p] = in_i[perm[p]], out_d[p] = in_d[perm[p]] (either output may be null).
 int launch_gather(long long nnz, const int *perm, const int *in_i, int *out_i,
                   const double *in_d, double *out_d, cudaStream_t stream);

@@ -81,7 +81,112 @@ struct sblas_batch_plan {
     void *mem;
     size_t mem_bytes;
     sblas::batch::Args args;
+    // one right-hand side, contiguous x and y, no row list or value
+    // permutation: sblas_batch_spmm runs the tile kernel over all matrices
+    // in one launch (multi-matrix tiles) instead of the warp-unit kernel
+    int multi;
+    void *multi_mem;
+    size_t multi_bytes;
+    sblas::MultiTileLaunch multi_launch;
 };
+
+namespace sblas {
+namespace batch {
+namespace {
+
+// Tiles, partitions and carries of the multi-matrix tile launch of a plan.
+int build_multi(sblas_batch_plan *p, const sblas_batch_matrix *mats, cudaStream_t st)
+{
+    const int nmat = p->nmat;
+    std::vector<int> tile0s(nmat + 1), part_off(nmat);
+    long long tiles = 0, parts = 0;
+    for (int i = 0; i < nmat; ++i) {
+        tile0s[i] = (int)tiles;
+        part_off[i] = (int)parts;
+        const long long nt = (long long)multi_tile_count(mats[i].nnz);
+        tiles += nt;
+        parts += nt + 1;
+        if (tiles > INT_MAX / 2 || parts > INT_MAX / 2) {
+            set_error(SBLAS_ERR_ARG, "batch too large for one launch (%lld tiles)", tiles);
+            return SBLAS_ERR_ARG;
+        }
+    }
+    tile0s[nmat] = (int)tiles;
+    const size_t b_mats = up256(multi_mat_bytes() * (size_t)nmat);
+    const size_t b_t0 = up256(sizeof(int) * (size_t)(nmat + 1));
+    const size_t b_part = up256(sizeof(int) * (size_t)parts);
+    const size_t b_carry = up256(sizeof(double) * (size_t)tiles);
+    const size_t total = b_mats + b_t0 + b_part + b_carry + 256;
+    cudaError_t e = cudaMalloc(&p->multi_mem, total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        p->multi_mem = nullptr;
+        set_error(SBLAS_ERR_ALLOC, "plan allocation of %zu bytes: %s", total,
+                  cudaGetErrorString(e));
+        return SBLAS_ERR_ALLOC;
+    }
+    p->multi_bytes = total;
+    unsigned char *b = static_cast<unsigned char *>(p->multi_mem);
+    std::vector<unsigned char> hm(multi_mat_bytes() * (size_t)nmat);
+    for (int i = 0; i < nmat; ++i) {
+        const sblas_batch_matrix &q = mats[i];
+        fill_multi_mat(hm.data() + multi_mat_bytes() * i, q.val, q.rowptr, q.col, q.x, q.y,
+                       q.nnz, q.m, tile0s[i], part_off[i], q.alpha, q.beta, p->val_kind);
+    }
+    MultiTileLaunch &L = p->multi_launch;
+    L.mats = b;
+    L.tile0s = reinterpret_cast<const int *>(b + b_mats);
+    L.nmat = nmat;
+    L.ntiles = (int)tiles;
+    int *part = reinterpret_cast<int *>(b + b_mats + b_t0);
+    L.part = part;
+    L.carry = reinterpret_cast<double *>(b + b_mats + b_t0 + b_part);
+    L.status = reinterpret_cast<int *>(b + b_mats + b_t0 + b_part + b_carry);
+    e = cudaMemcpyAsync(b, hm.data(), hm.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b + b_mats, tile0s.data(), sizeof(int) * (size_t)(nmat + 1),
+                            cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        set_error(SBLAS_ERR_CUDA, "plan upload: %s", cudaGetErrorString(e));
+        return SBLAS_ERR_CUDA;
+    }
+    // every matrix's tile partition; a matrix without nonzeros is one tile
+    // owning all its rows
+    std::vector<int> empty_part;
+    for (int i = 0; i < nmat; ++i) {
+        const sblas_batch_matrix &q = mats[i];
+        if (q.nnz > 0 && q.m > 0) {
+            const int rc = launch_tile_partition(q.m, q.nnz, q.rowptr, multi_tile_sigma(),
+                                                 part + part_off[i], st);
+            if (rc != SBLAS_OK) return rc;
+        } else {
+            empty_part.push_back(i);
+        }
+    }
+    std::vector<int> pairs(2 * empty_part.size());
+    for (size_t j = 0; j < empty_part.size(); ++j) {
+        pairs[2 * j] = 0;
+        pairs[2 * j + 1] = mats[empty_part[j]].m;
+        e = cudaMemcpyAsync(part + part_off[empty_part[j]], pairs.data() + 2 * j, 2 * sizeof(int),
+                            cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) {
+            set_error(SBLAS_ERR_CUDA, "plan upload: %s", cudaGetErrorString(e));
+            return SBLAS_ERR_CUDA;
+        }
+    }
+    // the host vectors above must outlive the copies
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_error(SBLAS_ERR_CUDA, "plan analysis: %s", cudaGetErrorString(e));
+        return SBLAS_ERR_CUDA;
+    }
+    p->multi = 1;
+    return SBLAS_OK;
+}
+
+}  // namespace
+}  // namespace batch
+}  // namespace sblas
 
 using namespace sblas;
 using namespace sblas::batch;
@@ -224,6 +329,19 @@ int sblas_batch_plan_create(int nmat, const sblas_batch_matrix *mats, int k, int
         std::free(p);
         return SBLAS_ERR_CUDA;
     }
+    bool multi = (k == 1);
+    for (int i = 0; i < nmat && multi; ++i)
+        multi = mats[i].row_ids == nullptr && mats[i].val_perm == nullptr && mats[i].ldx == 1 &&
+                mats[i].ldy == 1;
+    if (multi) {
+        const int rc = build_multi(p, mats, st);
+        if (rc != SBLAS_OK) {
+            if (p->multi_mem) cudaFree(p->multi_mem);
+            cudaFree(p->mem);
+            std::free(p);
+            return rc;
+        }
+    }
     *plan_out = p;
     return SBLAS_OK;
 }
@@ -235,7 +353,11 @@ int sblas_batch_plan_destroy(sblas_batch_plan *plan)
     int cur = -1;
     cudaGetDevice(&cur);
     if (cur != plan->device) cudaSetDevice(plan->device);
-    const cudaError_t e = cudaFree(plan->mem);
+    cudaError_t e = cudaFree(plan->mem);
+    if (plan->multi_mem) {
+        const cudaError_t e2 = cudaFree(plan->multi_mem);
+        if (e == cudaSuccess) e = e2;
+    }
     if (cur >= 0 && cur != plan->device) cudaSetDevice(cur);
     std::free(plan);
     if (e != cudaSuccess) {
@@ -255,7 +377,7 @@ int sblas_batch_plan_info(const sblas_batch_plan *plan, long long *units, int *s
     }
     if (units) *units = plan->nunits;
     if (s) *s = plan->s;
-    if (device_bytes) *device_bytes = plan->mem_bytes;
+    if (device_bytes) *device_bytes = plan->mem_bytes + plan->multi_bytes;
     return SBLAS_OK;
 }
 
@@ -266,6 +388,9 @@ int sblas_batch_spmm(const sblas_batch_plan *plan, void *stream)
         set_error(SBLAS_ERR_ARG, "null plan");
         return SBLAS_ERR_ARG;
     }
+    if (plan->multi)
+        return launch_multi_tile_spmv(plan->multi_launch, plan->val_kind,
+                                      static_cast<cudaStream_t>(stream));
     const cudaError_t e = dispatch(Op::SPMM, plan->k, plan->s, plan->val_kind, &plan->args,
                                    plan->nunits, plan->grid, nullptr,
                                    static_cast<cudaStream_t>(stream));

@@ -181,20 +181,104 @@ struct TileArgs {
     uint64_t wait_ns;     // limit of one bounded wait
 };
 
+// What a tile needs of the matrix it belongs to.
+struct MatView {
+    int m;
+    long long nnz;
+    long long tb;          // first nonzero of the tile, inside its matrix
+    const void *val;
+    const int *rowptr;
+    const int *col;
+    const double *x;
+    double *y;
+    double alpha;
+    double beta;
+    int use_tma;
+    int rp_tma;
+    const int *part;       // part[0], part[1]: the rows the tile owns, [R0, R1)
+    double *carry;         // the tile's carry slot
+};
+
+// Source of tiles: one matrix (TileArgs) or many (MultiArgs, below).  Both
+// give the total tile count, a tile's matrix and the tile's view of it.
+__device__ __forceinline__ int mat_of(const TileArgs &, int) { return 0; }
+
+template <int TILE>
+__device__ __forceinline__ MatView view_of(const TileArgs &a, int tile, int)
+{
+    return MatView{a.m,      a.nnz,   (long long)tile * TILE, a.val,   a.rowptr,
+                   a.col,    a.x,     a.y,                    a.alpha, a.beta,
+                   a.use_tma, a.rp_tma, a.row_part + tile,    a.carry + tile};
+}
+
+// One matrix of a multi-matrix launch (the batched single-right-hand-side
+// form): its tiles are global tiles [tile0, tile0 + ntiles), its partition
+// part[part_off .. part_off + ntiles].
+struct MultiMat {
+    const void *val;
+    const int *rowptr;
+    const int *col;
+    const double *x;
+    double *y;
+    long long nnz;
+    int m;
+    int tile0;
+    int part_off;
+    int use_tma;
+    int rp_tma;
+    double alpha;
+    double beta;
+};
+
+struct MultiArgs {
+    const MultiMat *mats;
+    const int *tile0s;    // [nmat + 1]: first global tile of every matrix, then the total
+    int nmat;
+    int ntiles;
+    const int *part;
+    double *carry;        // [ntiles], by global tile
+    int *status;
+    int stall;
+    uint64_t wait_ns;
+};
+
+__device__ __forceinline__ int mat_of(const MultiArgs &a, int tile)
+{
+    int lo = 0, hi = a.nmat - 1;   // last matrix with tile0 <= tile
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(a.tile0s + mid) <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int TILE>
+__device__ __forceinline__ MatView view_of(const MultiArgs &a, int tile, int mat)
+{
+    const MultiMat *M = a.mats + mat;
+    const int lt = tile - M->tile0;
+    return MatView{M->m,       M->nnz,    (long long)lt * TILE, M->val,  M->rowptr,
+                   M->col,     M->x,      M->y,                 M->alpha, M->beta,
+                   M->use_tma, M->rp_tma, a.part + M->part_off + lt, a.carry + tile};
+}
+
 // A bounded wait gave up: the launch's status word and the sticky word.
-__device__ __forceinline__ void report_timeout(const TileArgs &a)
+template <class Src>
+__device__ __forceinline__ void report_timeout(const Src &a)
 {
     atomicExch(a.status, DEV_ERR_TIMEOUT);
     atomicOr(&g_sticky_error, DEV_ERR_TIMEOUT);
 }
 
-// y epilogue for one finished row value v.
+// y epilogue for one finished row value v.  AB = 3: alpha and beta known
+// only at run time (matrices of a multi-matrix launch each have their own).
 template <int AB>
 __device__ __forceinline__ double finish_row(double v, double alpha, double beta,
                                              const double *yp)
 {
     if (AB == 0) return v;                               // alpha = 1, beta = 0
     if (AB == 1) return alpha * v;                       // beta = 0
+    if (AB == 3 && beta == 0.0) return alpha == 1.0 ? v : alpha * v;
     return fma(alpha, v, beta * __ldg(yp));              // general
 }
 
@@ -228,13 +312,13 @@ struct Smem {
 // of the 32 lanes.  Completion: the stage's `full` mbarrier (one arrive with
 // the byte count, after the plain stores).
 template <int SIGMA, int VK>
-__device__ __forceinline__ void produce_tile(const TileArgs &a, const Smem<SIGMA, VK> &sm,
-                                             int tile, int s, int R0, int R1, int lane,
+__device__ __forceinline__ void produce_tile(const MatView &a, const Smem<SIGMA, VK> &sm,
+                                             int mat, int s, int R0, int R1, int lane,
                                              uint64_t pol)
 {
     using L = Layout<SIGMA, VK>;
     using VT = typename ValTraits<VK>::T;
-    const long long tb = (long long)tile * L::TILE;
+    const long long tb = a.tb;
     const int cnt = (int)((a.nnz - tb < L::TILE) ? (a.nnz - tb) : L::TILE);
     const int vdone = a.use_tma ? (int)((((long long)cnt * L::VB) & ~15ll) / (L::VB ? L::VB : 1)) : 0;
     const int cdone = a.use_tma ? (int)((((long long)cnt * 4) & ~15ll) / 4) : 0;
@@ -262,7 +346,7 @@ __device__ __forceinline__ void produce_tile(const TileArgs &a, const Smem<SIGMA
         meta[0] = R0;
         meta[1] = R1;
         meta[2] = base;
-        meta[3] = fits;
+        meta[3] = fits | (mat << 1);   // the tile's matrix rides with the flag
     }
     __syncwarp();
     if (lane == 0) {
@@ -300,30 +384,32 @@ __device__ __forceinline__ double widen_f32(float v)
 // buffer of the tile's parity; the chunk's head (first segment of a row
 // begun earlier) and tail (partial of the row crossing the chunk end) are
 // published for the epilogue warp of the tile's parity.  No CTA-wide barrier.
-template <int SIGMA, int VK, int AB>
-__device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+template <int SIGMA, int VK, int AB, class Src>
+__device__ __forceinline__ void compute_warp(const Src &src, const Smem<SIGMA, VK> &sm,
                                              int cw, int lane, uint64_t pol_x)
 {
     using L = Layout<SIGMA, VK>;
     using VT = typename ValTraits<VK>::T;
     constexpr int TILE = L::TILE;
     const int t = cw * 32 + lane;
-    const double alpha = a.alpha, beta = a.beta;
-    for (int i = 0, tile = blockIdx.x; tile < a.ntiles; ++i, tile += gridDim.x) {
+    for (int i = 0, tile = blockIdx.x; tile < src.ntiles; ++i, tile += gridDim.x) {
         const int s = i % STAGES;
         const int p = i & 1;
-        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), a.wait_ns);
+        bool ok = ptx::mbar_wait_bounded(sm.full(s), (uint32_t)((i / STAGES) & 1), src.wait_ns);
         if (i >= 2)
             ok = ok && ptx::mbar_wait_bounded(sm.cempty(p), (uint32_t)(((i - 2) / 2) & 1),
-                                              a.wait_ns);
+                                              src.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) report_timeout(a);
+            if (lane == 0) report_timeout(src);
             return;
         }
         const int *meta = sm.meta(s);
         const int R0 = meta[0], R1 = meta[1], rbase = meta[2];
-        const bool fits = meta[3] != 0;
-        const long long tb = (long long)tile * TILE;
+        const bool fits = (meta[3] & 1) != 0;
+        const int mat = meta[3] >> 1;
+        const MatView a = view_of<TILE>(src, tile, mat);
+        const double alpha = a.alpha, beta = a.beta;
+        const long long tb = a.tb;
         const int cnt_tile = (int)((a.nnz - tb < TILE) ? (a.nnz - tb) : TILE);
         const VT *vst = sm.val(s);
         const int *cst = sm.col(s);
@@ -447,7 +533,7 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
             cm[0] = R0;
             cm[1] = R1;
             cm[2] = fits;
-            cm[3] = tile;
+            cm[3] = mat;
         }
         __syncwarp();
         if (lane == 0) {
@@ -460,35 +546,40 @@ __device__ __forceinline__ void compute_warp(const TileArgs &a, const Smem<SIGMA
 // Producer warp: stages the CTA's tiles into the STAGES-deep ring, each as
 // soon as the compute warps release its stage; the tile's partition entries
 // are loaded before that wait, so their latency hides behind it.
-template <int SIGMA, int VK>
-__device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+template <int SIGMA, int VK, class Src>
+__device__ __forceinline__ void producer_warp(const Src &src, const Smem<SIGMA, VK> &sm,
                                               int lane, uint64_t pol_stream)
 {
-    if (a.stall) return;   // test hook: nothing is staged, the other warps' waits run out
+    constexpr int TILE = Layout<SIGMA, VK>::TILE;
+    if (src.stall) return;   // test hook: nothing is staged, the other warps' waits run out
     int issued[STAGES];
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) issued[s] = 0;
     for (int s = 0; s < STAGES; ++s) {
         const int t = blockIdx.x + s * (int)gridDim.x;
-        if (t < a.ntiles) {
-            produce_tile<SIGMA, VK>(a, sm, t, s, __ldg(a.row_part + t), __ldg(a.row_part + t + 1),
-                                    lane, pol_stream);
+        if (t < src.ntiles) {
+            const int mat = mat_of(src, t);
+            const MatView v = view_of<TILE>(src, t, mat);
+            produce_tile<SIGMA, VK>(v, sm, mat, s, __ldg(v.part), __ldg(v.part + 1), lane,
+                                    pol_stream);
             ++issued[s];
         }
     }
-    for (int i = 0, nt = blockIdx.x + STAGES * (int)gridDim.x; nt < a.ntiles;
+    for (int i = 0, nt = blockIdx.x + STAGES * (int)gridDim.x; nt < src.ntiles;
          ++i, nt += gridDim.x) {
         const int s = i % STAGES;
-        const int R0 = __ldg(a.row_part + nt);
-        const int R1 = __ldg(a.row_part + nt + 1);
+        const int mat = mat_of(src, nt);
+        const MatView v = view_of<TILE>(src, nt, mat);
+        const int R0 = __ldg(v.part);
+        const int R1 = __ldg(v.part + 1);
         const bool ok = ptx::mbar_wait_bounded(sm.empty(s), (uint32_t)((i / STAGES) & 1),
-                                               a.wait_ns);
+                                               src.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) report_timeout(a);
+            if (lane == 0) report_timeout(src);
             break;
         }
         ptx::fence_proxy_async_smem();
-        produce_tile<SIGMA, VK>(a, sm, nt, s, R0, R1, lane, pol_stream);
+        produce_tile<SIGMA, VK>(v, sm, mat, s, R0, R1, lane, pol_stream);
         ++issued[s];
     }
     // the CTA may exit only when no copy into its shared memory is in flight
@@ -509,27 +600,29 @@ __device__ __forceinline__ void producer_warp(const TileArgs &a, const Smem<SIGM
 //   of the chunk where the row ends, to a complete row, or to the tile carry;
 //   head pass: head + carry-in, one converged add per chunk;
 //   epilogue: alpha/beta once per row, coalesced stores of y.
-template <int SIGMA, int VK, int AB>
-__device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGMA, VK> &sm,
+template <int SIGMA, int VK, int AB, class Src>
+__device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, VK> &sm,
                                               int par, int lane)
 {
     constexpr int PER = NCW;  // tails reduced per lane
-    const double alpha = a.alpha, beta = a.beta;
+    constexpr int TILE = Layout<SIGMA, VK>::TILE;
     double *cin = sm.cin(par);
     // this warp takes the tiles of parity `par` (the CTA's tiles i = par,
     // par + 2, ...): the carry buffers are double-buffered by that parity
-    for (int i = par, tile = blockIdx.x + par * (int)gridDim.x; tile < a.ntiles;
+    for (int i = par, tile = blockIdx.x + par * (int)gridDim.x; tile < src.ntiles;
          i += 2, tile += 2 * (int)gridDim.x) {
         const int p = i & 1;
         const bool ok = ptx::mbar_wait_bounded(sm.cfull(p), (uint32_t)((i / 2) & 1),
-                                               a.wait_ns);
+                                               src.wait_ns);
         if (!__all_sync(0xffffffffu, ok)) {
-            if (lane == 0) report_timeout(a);
+            if (lane == 0) report_timeout(src);
             break;
         }
         const int *cm = sm.cmeta(p);
         const int R0 = cm[0], R1 = cm[1];
         const bool fits = cm[2] != 0;
+        const MatView a = view_of<TILE>(src, tile, cm[3]);
+        const double alpha = a.alpha, beta = a.beta;
         double *rval = sm.rval(p);
         const double *tailv = sm.tailv(p);
         const int *tailk = sm.tailk(p);
@@ -543,14 +636,14 @@ __device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGM
                 if (after < TC && headk[after] == key) {
                     cin[after] = total;                      // joins a head
                 } else if (after >= TC && key == R1) {
-                    a.carry[tile] = total;                   // continues in next tile
+                    *a.carry = total;                        // continues in next tile
                 } else if (fits) {
                     rval[key - R0] = total;                  // complete row
                 } else {
                     a.y[key] = finish_row<AB>(total, alpha, beta, a.y + key);
                 }
             };
-            if (lane == 0) a.carry[tile] = 0.0;
+            if (lane == 0) *a.carry = 0.0;
             __syncwarp();
             const int base = lane * PER;          // first thread of this lane's tails
             double acc = 0.0;
@@ -632,8 +725,8 @@ __device__ __forceinline__ void epilogue_warp(const TileArgs &a, const Smem<SIGM
     }
 }
 
-template <int SIGMA, int VK, int AB>
-__global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a)
+template <int SIGMA, int VK, int AB, class Src>
+__global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const Src a)
 {
     using L = Layout<SIGMA, VK>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -656,11 +749,11 @@ __global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const TileArgs a
     for (int i = tid; i < 2 * TC; i += CTA_THREADS) sm.cin(0)[i] = 0.0;
     __syncthreads();
     if (warp == NCW)
-        producer_warp<SIGMA, VK>(a, sm, lane, ptx::policy_evict_first());
+        producer_warp<SIGMA, VK, Src>(a, sm, lane, ptx::policy_evict_first());
     else if (warp > NCW)
-        epilogue_warp<SIGMA, VK, AB>(a, sm, warp - NCW - 1, lane);
+        epilogue_warp<SIGMA, VK, AB, Src>(a, sm, warp - NCW - 1, lane);
     else
-        compute_warp<SIGMA, VK, AB>(a, sm, warp, lane, ptx::policy_evict_last());
+        compute_warp<SIGMA, VK, AB, Src>(a, sm, warp, lane, ptx::policy_evict_last());
 }
 
 // part[k] = number of rows r with rowptr[r+1] <= k*TILE (k = 1..ntiles-1);
@@ -762,6 +855,29 @@ __global__ void scale_y_kernel(int m, double beta, double *__restrict__ y)
         y[i] = (beta == 0.0) ? 0.0 : beta * y[i];
 }
 
+// tile_fixup_kernel for a multi-matrix launch: global tile k, its matrix's
+// own tiles and partition.
+__global__ void multi_fixup_kernel(const MultiArgs a, long long tile)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.ntiles) return;
+    if (*a.status != 0) return;
+    const MultiMat *M = a.mats + mat_of(a, k);
+    const int lt = k - M->tile0;
+    if (lt == 0) return;                                        // a matrix's first tile
+    const int *part = a.part + M->part_off;
+    const int r = part[lt];
+    if (part[lt + 1] <= r) return;                              // row r ends later
+    if ((long long)__ldg(M->rowptr + r) >= (long long)lt * tile) return;   // starts here
+    int j = lt - 1;
+    double c = a.carry[M->tile0 + j];
+    while (j >= 1 && part[j] == part[j + 1]) {
+        c += a.carry[M->tile0 + j - 1];
+        --j;
+    }
+    M->y[r] = fma(M->alpha, c, M->y[r]);
+}
+
 // ---------------- compiled shapes -----------------------------------------
 constexpr int kSigmas[] = {11, 15, 19, 23, 27};
 constexpr int kNumSigmas = sizeof(kSigmas) / sizeof(kSigmas[0]);
@@ -770,11 +886,11 @@ constexpr int kNumSigmas = sizeof(kSigmas) / sizeof(kSigmas[0]);
 // resident CTAs per SM (0 = not configured yet); host threads may launch
 // concurrently.  Configuring also loads the kernel onto the device under
 // lazy module loading.
-template <int SIGMA, int VK, int AB>
+template <int SIGMA, int VK, int AB, class Src = TileArgs>
 int configure_shape(int *out_bps)
 {
     using L = Layout<SIGMA, VK>;
-    auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
+    auto kfn = tile_spmv_kernel<SIGMA, VK, AB, Src>;
     constexpr int kMaxDev = 64;
     static std::atomic<int> blocks_per_sm[kMaxDev];
     static std::mutex config_mu;
@@ -805,13 +921,13 @@ int configure_shape(int *out_bps)
     return SBLAS_OK;
 }
 
-template <int SIGMA, int VK, int AB>
-int launch_shape(const TileArgs &a, cudaStream_t stream)
+template <int SIGMA, int VK, int AB, class Src = TileArgs>
+int launch_shape(const Src &a, cudaStream_t stream)
 {
     using L = Layout<SIGMA, VK>;
-    auto kfn = tile_spmv_kernel<SIGMA, VK, AB>;
+    auto kfn = tile_spmv_kernel<SIGMA, VK, AB, Src>;
     int bps = 0;
-    const int rc = configure_shape<SIGMA, VK, AB>(&bps);
+    const int rc = configure_shape<SIGMA, VK, AB, Src>(&bps);
     if (rc != SBLAS_OK) return rc;
     const int grid = min(a.ntiles, bps * device_num_sms());
     kfn<<<grid, CTA_THREADS, L::TOTAL, stream>>>(a);
@@ -990,6 +1106,79 @@ int tile_preload_f64(int sigma)
     SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, tile_fixup_kernel));
     SBLAS_CUDA_TRY(cudaFuncGetAttributes(&fa, scale_y_kernel));
     return SBLAS_OK;
+}
+
+int multi_tile_sigma() { return 11; }
+
+size_t multi_tile_count(long long nnz)
+{
+    const long long tile = (long long)TC * multi_tile_sigma();
+    return nnz <= 0 ? 1 : (size_t)((nnz + tile - 1) / tile);
+}
+
+int launch_tile_partition(int m, long long nnz, const int *rowptr, int sigma, int *part,
+                          cudaStream_t stream)
+{
+    // launch_tile_analyse writes the partition after the status word
+    return launch_tile_analyse(m, nnz, rowptr, sigma,
+                               reinterpret_cast<unsigned char *>(part) - kStatusBytes, stream);
+}
+
+int launch_multi_tile_spmv(const MultiTileLaunch &L, int val_kind, cudaStream_t stream)
+{
+    if (L.ntiles <= 0) return SBLAS_OK;
+    MultiArgs a;
+    a.mats = static_cast<const MultiMat *>(L.mats);
+    a.tile0s = L.tile0s;
+    a.nmat = L.nmat;
+    a.ntiles = L.ntiles;
+    a.part = L.part;
+    a.carry = L.carry;
+    a.status = L.status;
+    a.stall = g_stall.load(std::memory_order_relaxed);
+    a.wait_ns = g_wait_ns.load(std::memory_order_relaxed);
+    SBLAS_CUDA_TRY(cudaMemsetAsync(L.status, 0, sizeof(int), stream));
+    int rc;
+    switch (val_kind) {
+    case VAL_F64: rc = launch_shape<11, VAL_F64, 3, MultiArgs>(a, stream); break;
+    case VAL_F32: rc = launch_shape<11, VAL_F32, 3, MultiArgs>(a, stream); break;
+    case VAL_PATTERN: rc = launch_shape<11, VAL_PATTERN, 3, MultiArgs>(a, stream); break;
+    default:
+        set_error(SBLAS_ERR_ARG, "unknown value kind %d", val_kind);
+        return SBLAS_ERR_ARG;
+    }
+    if (rc != SBLAS_OK) return rc;
+    if (a.ntiles > 1) {
+        const int threads = 256;
+        multi_fixup_kernel<<<(a.ntiles + threads - 1) / threads, threads, 0, stream>>>(
+            a, (long long)TC * multi_tile_sigma());
+        SBLAS_CUDA_TRY(cudaGetLastError());
+    }
+    return SBLAS_OK;
+}
+
+size_t multi_mat_bytes() { return sizeof(MultiMat); }
+
+void fill_multi_mat(void *dst, const void *val, const int *rowptr, const int *col,
+                    const double *x, double *y, long long nnz, int m, int tile0, int part_off,
+                    double alpha, double beta, int val_kind)
+{
+    MultiMat M;
+    M.val = val;
+    M.rowptr = rowptr;
+    M.col = col;
+    M.x = x;
+    M.y = y;
+    M.nnz = nnz;
+    M.m = m;
+    M.tile0 = tile0;
+    M.part_off = part_off;
+    const uintptr_t vb = reinterpret_cast<uintptr_t>(val), cb = reinterpret_cast<uintptr_t>(col);
+    M.use_tma = ((val_kind == VAL_PATTERN || (vb & 15) == 0) && (cb & 15) == 0) ? 1 : 0;
+    M.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
+    M.alpha = alpha;
+    M.beta = beta;
+    *static_cast<MultiMat *>(dst) = M;
 }
 
 void set_wait_limit_ns(unsigned long long ns)

@@ -153,14 +153,72 @@ def csc_to_csr(m: int, n: int, colptr: torch.Tensor, rowidx: torch.Tensor,
     return rowptr, col, oval
 
 
+def cscmv_workspace_bytes(m: int, n: int, nnz: int) -> int:
+    return int(_lib.load().sblas_cscmv_workspace_bytes(m, n, nnz))
+
+
 def cscmv(colptr: torch.Tensor, rowidx: torch.Tensor, val: torch.Tensor, x: torch.Tensor,
-          y: torch.Tensor, alpha: float = 1.0, beta: float = 0.0) -> torch.Tensor:
-    """y = alpha*A*x + beta*y with A in CSC: device transpose to CSR, then the
-    atomic-free tile kernel."""
+          y: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+          work: torch.Tensor | None = None) -> torch.Tensor:
+    """y = alpha*A*x + beta*y with A in CSC (sblas_dcscmv): the row-ordered
+    structure by a stable bucket sort (inspector), then the values gathered
+    into row order and the CSR tile kernel: atomic-free, bit-reproducible.
+    work: optional uint8 device buffer of cscmv_workspace_bytes(m, n, nnz)."""
+    dev = _require_cuda(colptr, rowidx, val, x, y, work)
+    for what, t, dt in (("colptr", colptr, torch.int32), ("rowidx", rowidx, torch.int32),
+                        ("val", val, torch.float64), ("x", x, torch.float64),
+                        ("y", y, torch.float64)):
+        _require_dtype(what, t, dt)
     m = y.numel()
     n = colptr.numel() - 1
-    rp, c, v = csc_to_csr(m, n, colptr, rowidx, val)
-    return csrmv(rp, c, v, x, y, alpha, beta, n=n)
+    nnz = rowidx.numel()
+    _require_len("val", val, nnz)
+    _require_len("x", x, n)
+    wb = work.numel() * work.element_size() if work is not None else 0
+    lib = _lib.load()
+    with torch.cuda.device(dev):
+        rc = lib.sblas_dcscmv(m, n, nnz, float(alpha), _ptr(val), _ptr(colptr), _ptr(rowidx),
+                              _ptr(x), float(beta), _ptr(y), _ptr(work), wb, _stream_ptr(dev))
+    _lib.check(rc)
+    return y
+
+
+class CscPlan:
+    """A CSC pattern (int32 colptr, rowidx) analysed once (sblas_csc_analyse:
+    the row-ordered structure, the permutation to it and the tile
+    partition, held in the plan's workspace); each call runs only the
+    executor (sblas_dcscmv_analysed: the values gathered into row order and
+    the tile kernel), with the values, x and y given per call."""
+
+    def __init__(self, m: int, colptr: torch.Tensor, rowidx: torch.Tensor):
+        dev = _require_cuda(colptr, rowidx)
+        _require_dtype("colptr", colptr, torch.int32)
+        _require_dtype("rowidx", rowidx, torch.int32)
+        self.m, self.n, self.nnz = int(m), colptr.numel() - 1, rowidx.numel()
+        self.colptr, self.rowidx, self.device = colptr, rowidx, dev
+        lib = _lib.load()
+        self.work_bytes = int(lib.sblas_cscmv_workspace_bytes(self.m, self.n, self.nnz))
+        self.work = torch.empty(self.work_bytes, dtype=torch.uint8, device=dev)
+        with torch.cuda.device(dev):
+            rc = lib.sblas_csc_analyse(self.m, self.n, self.nnz, _ptr(colptr), _ptr(rowidx),
+                                       _ptr(self.work), self.work_bytes, _stream_ptr(dev))
+        _lib.check(rc)
+
+    def __call__(self, val: torch.Tensor, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0,
+                 beta: float = 0.0) -> torch.Tensor:
+        if _require_cuda(val, x, y) != self.device:
+            raise ValueError("val, x and y must be on the plan's device")
+        for what, t in (("val", val), ("x", x), ("y", y)):
+            _require_dtype(what, t, torch.float64)
+        _require_len("val", val, self.nnz)
+        _require_len("x", x, self.n)
+        if y.numel() != self.m:
+            raise ValueError("y must have m entries")
+        rc = _lib.load().sblas_dcscmv_analysed(self.m, self.n, self.nnz, float(alpha), _ptr(val),
+                                               _ptr(x), float(beta), _ptr(y), _ptr(self.work),
+                                               self.work_bytes, _stream_ptr(self.device))
+        _lib.check(rc)
+        return y
 
 
 class CsrPlan:

@@ -158,13 +158,36 @@ SBLAS_API int sblas_dcoomv(int m, int n, long long nnz, double alpha, const doub
                  double *y, int *rowptr_work, int sigma, void *work, size_t work_bytes,
                  void *stream);
 
-/* CSC -> CSR on the device (stable; columns ascending inside each row).
+/* CSC -> CSR on the device (stable; columns ascending inside each row): a
+ * least-significant-digit bucket sort by row, 8-bit digits (three passes
+ * up to 16M rows).
  * work: sblas_csc_to_csr_workspace_bytes(m, n, nnz) bytes. */
 SBLAS_API size_t sblas_csc_to_csr_workspace_bytes(int m, int n, long long nnz);
 SBLAS_API int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
                      const int *csc_colptr, const int *csc_row, double *csr_val,
                      int *csr_rowptr, int *csr_col, void *work, size_t work_bytes,
                      void *stream);
+
+/* y = alpha*A*x + beta*y with A in CSC on the device (colptr[n + 1],
+ * rowidx[nnz], val[nnz]), the device form of spMV_mgpu_baseline_csc
+ * (src/dspmv_mgpu_baseline_csc.cu:131-135 runs it as a transposed csrmv).
+ * Inspector: a stable bucket sort of the entries by row gives A's row-ordered
+ * structure and the permutation to it (sblas_csc_analyse, into `work`);
+ * executor: the values gathered into row order and the CSR tile kernel
+ * (sblas_dcscmv_analysed, with the same work, colptr/rowidx unchanged):
+ * no atomics, bit-reproducible.  sblas_dcscmv runs both.  Rows need not be
+ * sorted inside a column.  work: sblas_cscmv_workspace_bytes(m, n, nnz)
+ * bytes, 256-byte aligned (sblas_dcscmv: or NULL for a library-owned
+ * buffer).  A bounded wait that gave up is reported by sblas_stream_status. */
+SBLAS_API size_t sblas_cscmv_workspace_bytes(int m, int n, long long nnz);
+SBLAS_API int sblas_dcscmv(int m, int n, long long nnz, double alpha, const double *val,
+                           const int *colptr, const int *rowidx, const double *x, double beta,
+                           double *y, void *work, size_t work_bytes, void *stream);
+SBLAS_API int sblas_csc_analyse(int m, int n, long long nnz, const int *colptr,
+                                const int *rowidx, void *work, size_t work_bytes, void *stream);
+SBLAS_API int sblas_dcscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
+                                    const double *x, double beta, double *y, void *work,
+                                    size_t work_bytes, void *stream);
 
 /* Row-sorted COO row indices -> CSR row pointer (int[m + 1]). */
 SBLAS_API int sblas_coo_rows_to_rowptr(int m, long long nnz, const int *coo_row, int *rowptr,
