@@ -90,6 +90,8 @@ SIGNATURES: dict[str, tuple] = {
                                     _vp]),
     "sblas_dcscmv_analysed": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_double, _vp, _vp,
                                         C.c_double, _vp, _vp, C.c_size_t, _vp]),
+    "sblas_csc_bind_values": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _vp, _vp, C.c_size_t,
+                                        _vp]),
     "sblas_nnz_partition": (C.c_int, [C.c_int, C.c_longlong, _ip, C.c_int, C.c_void_p]),
     "sblas_part_rowptr": (C.c_int, [_ip, C.c_void_p, _ip]),
     "sblas_merge_parts": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_double, _dp]),

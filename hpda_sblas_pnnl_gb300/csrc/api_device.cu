@@ -324,12 +324,24 @@ int sblas_csc_analyse(int m, int n, long long nnz, const int *colptr, const int 
                               static_cast<cudaStream_t>(stream));
 }
 
+int sblas_csc_bind_values(int m, int n, long long nnz, const double *val, void *work,
+                          size_t work_bytes, void *stream)
+{
+    clear_error();
+    if (nnz > 0 && val == nullptr) {
+        set_error(SBLAS_ERR_ARG, "null device pointer");
+        return SBLAS_ERR_ARG;
+    }
+    return launch_csc_bind_values(m, n, nnz, val, work, work_bytes,
+                                  static_cast<cudaStream_t>(stream));
+}
+
 int sblas_dcscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
                           const double *x, double beta, double *y, void *work, size_t work_bytes,
                           void *stream)
 {
     clear_error();
-    if (m > 0 && (y == nullptr || (nnz > 0 && (val == nullptr || x == nullptr)))) {
+    if (m > 0 && (y == nullptr || (nnz > 0 && x == nullptr))) {
         set_error(SBLAS_ERR_ARG, "null device pointer");
         return SBLAS_ERR_ARG;
     }

@@ -13,6 +13,10 @@
 //                         its payloads, then written out so that consecutive
 //                         threads write consecutive positions of one digit's run
 //                         (about TILE / nb entries): coalesced stores.
+//                         Every key and payload load of a tile is issued
+//                         before the first is used, and tiles are small
+//                         (~51 KB of shared memory) so that several CTAs per
+//                         SM hide the memory latency.
 // Entries keep their input order inside every digit (tiles in order, warps in
 // order inside a tile, entries in order inside a warp): a least-significant-
 // digit sequence of passes is a stable sort.  Counts are integers and
@@ -32,9 +36,9 @@ namespace {
 
 constexpr int NW = 8;                   // warps per CTA
 constexpr int THREADS = NW * 32;
-constexpr int ITER = 16;                // entries per lane per tile
-constexpr int WSPAN = 32 * ITER;        // entries of one warp in a tile (512)
-constexpr int TILE = NW * WSPAN;        // entries per CTA tile (4096)
+constexpr int ITER = 8;                 // entries per lane per tile
+constexpr int WSPAN = 32 * ITER;        // entries of one warp in a tile (256)
+constexpr int TILE = NW * WSPAN;        // entries per CTA tile (2048)
 constexpr int MAXB = 256;               // digit values per pass (8-bit digits)
 
 __host__ __device__ inline long long num_tiles(long long n) { return (n + TILE - 1) / TILE; }
@@ -215,7 +219,7 @@ struct Payload {
 //     members key_out, a_out, b_out, d_out: the pass's outputs (a, b, d may
 //     be null: not carried).
 template <class Op>
-__global__ void __launch_bounds__(THREADS, 2) bucket_scatter_kernel(const Op op, long long n,
+__global__ void __launch_bounds__(THREADS, 3) bucket_scatter_kernel(const Op op, long long n,
                                                                  int shift, int nb, int ntiles,
                                                                  const int *__restrict__ table)
 {
@@ -236,12 +240,21 @@ __global__ void __launch_bounds__(THREADS, 2) bucket_scatter_kernel(const Op op,
     for (int i = tid; i < NW * MAXB; i += THREADS) wcnt[i] = 0;
     for (int d = tid; d < nb; d += THREADS)
         gbase[d] = __ldg(table + (long long)d * ntiles + blockIdx.x);
-    // this warp's keys, all loads in flight at once
+    // this warp's keys and payloads, every load in flight before the first
+    // is used (the kernel is bound by memory latency otherwise)
     int kr[ITER];
+    Payload pl[ITER];
+    typename Op::State st{};
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
         const long long e = wbeg + (long long)i * 32 + lane;
         kr[i] = e < n ? op.key(e) : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < ITER; ++i) {
+        const long long e0 = wbeg + (long long)i * 32;
+        pl[i] = (e0 < n) ? op.load(st, e0, lane, e0 + lane < n, e0 + lane)   // warp-uniform
+                         : Payload{0, 0, 0.0};
     }
     __syncthreads();
     unsigned short *mycnt = wcnt + w * MAXB;
@@ -288,23 +301,17 @@ __global__ void __launch_bounds__(THREADS, 2) bucket_scatter_kernel(const Op op,
     if (tid < nb) toff[tid] = before + v - total;
     __syncthreads();
     // the tile in digit order, with its payloads, in shared memory
-    typename Op::State st{};
     const bool ha = op.a_out != nullptr, hb = op.b_out != nullptr, hd = op.d_out != nullptr;
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
-        const long long e0 = wbeg + (long long)i * 32;
-        if (e0 < n) {                                              // warp-uniform
-            const long long e = e0 + lane;
-            const bool valid = e < n;
-            const Payload pl = op.load(st, e0, lane, valid, e);
-            if (valid) {
-                const int d = digit_of(kr[i], shift, nb);
-                const int slot = toff[d] + mycnt[d] + loc[w * WSPAN + i * 32 + lane];
-                st_key[slot] = kr[i];
-                if (ha) st_a[slot] = pl.a;
-                if (hb) st_b[slot] = pl.b;
-                if (hd) st_d[slot] = pl.d;
-            }
+        const long long e = wbeg + (long long)i * 32 + lane;
+        if (e < n) {
+            const int d = digit_of(kr[i], shift, nb);
+            const int slot = toff[d] + mycnt[d] + loc[w * WSPAN + i * 32 + lane];
+            st_key[slot] = kr[i];
+            if (ha) st_a[slot] = pl[i].a;
+            if (hb) st_b[slot] = pl[i].b;
+            if (hd) st_d[slot] = pl[i].d;
         }
     }
     __syncthreads();

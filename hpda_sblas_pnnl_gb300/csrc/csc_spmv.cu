@@ -13,8 +13,10 @@
 //              writes) and the CSR tile kernel: its segmented sums and carry
 //              fix-up in a fixed order, no atomics, bit-reproducible.
 // sblas_dcscmv runs both; sblas_csc_analyse / sblas_dcscmv_analysed split
-// them for a pattern used many times (the executor alone then costs about
-// one value gather more than a CSR product).
+// them for a pattern used many times (the executor then costs one value
+// gather, a random read of every value, more than a CSR product), and
+// sblas_csc_bind_values keeps one set of values in row order inside the
+// analysis, so that products with those values cost a CSR product alone.
 #include "sblas_internal.h"
 
 namespace sblas {
@@ -110,6 +112,20 @@ int launch_csc_analyse(int m, int n, long long nnz, const int *colptr, const int
     return launch_tile_analyse(m, nnz, rowptr, kCscSigma, w + L.tile, stream);
 }
 
+int launch_csc_bind_values(int m, int n, long long nnz, const double *val, void *work,
+                           size_t work_bytes, cudaStream_t stream)
+{
+    if (m <= 0 || nnz <= 0) return SBLAS_OK;
+    if (!check_work(m, n, nnz, work, work_bytes)) return SBLAS_ERR_ARG;
+    const CscLayout L = csc_layout(m, n, nnz);
+    unsigned char *w = static_cast<unsigned char *>(work);
+    const long long want = (nnz + 255) / 256, cap = 16LL * device_num_sms();
+    gather_rows_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, stream>>>(
+        nnz, reinterpret_cast<const int *>(w + L.perm), val, reinterpret_cast<double *>(w + L.val));
+    SBLAS_CUDA_TRY(cudaGetLastError());
+    return SBLAS_OK;
+}
+
 int launch_cscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
                           const double *x, double beta, double *y, void *work,
                           size_t work_bytes, cudaStream_t stream)
@@ -124,10 +140,10 @@ int launch_cscmv_analysed(int m, int n, long long nnz, double alpha, const doubl
     const CscLayout L = csc_layout(m, n, nnz);
     unsigned char *w = static_cast<unsigned char *>(work);
     double *rval = reinterpret_cast<double *>(w + L.val);
-    const long long want = (nnz + 255) / 256, cap = 16LL * device_num_sms();
-    gather_rows_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, stream>>>(
-        nnz, reinterpret_cast<const int *>(w + L.perm), val, rval);
-    SBLAS_CUDA_TRY(cudaGetLastError());
+    if (val != nullptr) {   // new values: into row order (else the bound ones)
+        const int rc = launch_csc_bind_values(m, n, nnz, val, work, work_bytes, stream);
+        if (rc != SBLAS_OK) return rc;
+    }
     return launch_tile_spmv(m, n, nnz, alpha, rval, VAL_F64,
                             reinterpret_cast<const int *>(w + L.rowptr),
                             reinterpret_cast<const int *>(w + L.col), x, beta, y, kCscSigma,

@@ -137,6 +137,8 @@ int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
 size_t cscmv_workspace_bytes(int m, int n, long long nnz);
 int launch_csc_analyse(int m, int n, long long nnz, const int *colptr, const int *rowidx,
                        void *work, size_t work_bytes, cudaStream_t stream);
+int launch_csc_bind_values(int m, int n, long long nnz, const double *val, void *work,
+                           size_t work_bytes, cudaStream_t stream);
 int launch_cscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
                           const double *x, double beta, double *y, void *work,
                           size_t work_bytes, cudaStream_t stream);

@@ -188,7 +188,9 @@ class CscPlan:
     the row-ordered structure, the permutation to it and the tile
     partition, held in the plan's workspace); each call runs only the
     executor (sblas_dcscmv_analysed: the values gathered into row order and
-    the tile kernel), with the values, x and y given per call."""
+    the tile kernel), with the values, x and y given per call; bind() keeps
+    one set of values in row order (calls with val=None then skip the
+    gather)."""
 
     def __init__(self, m: int, colptr: torch.Tensor, rowidx: torch.Tensor):
         dev = _require_cuda(colptr, rowidx)
@@ -204,8 +206,23 @@ class CscPlan:
                                        _ptr(self.work), self.work_bytes, _stream_ptr(dev))
         _lib.check(rc)
 
-    def __call__(self, val: torch.Tensor, x: torch.Tensor, y: torch.Tensor, alpha: float = 1.0,
-                 beta: float = 0.0) -> torch.Tensor:
+    def bind(self, val: torch.Tensor) -> None:
+        """Keeps these values (CSC order) in row order inside the plan: calls
+        with val=None then use them and skip the per-call gather."""
+        if _require_cuda(val) != self.device:
+            raise ValueError("val must be on the plan's device")
+        _require_dtype("val", val, torch.float64)
+        _require_len("val", val, self.nnz)
+        rc = _lib.load().sblas_csc_bind_values(self.m, self.n, self.nnz, _ptr(val),
+                                               _ptr(self.work), self.work_bytes,
+                                               _stream_ptr(self.device))
+        _lib.check(rc)
+        self.bound = True
+
+    def __call__(self, val: torch.Tensor | None, x: torch.Tensor, y: torch.Tensor,
+                 alpha: float = 1.0, beta: float = 0.0) -> torch.Tensor:
+        if val is None and not getattr(self, "bound", False):
+            raise ValueError("no values: pass val or bind() them first")
         if _require_cuda(val, x, y) != self.device:
             raise ValueError("val, x and y must be on the plan's device")
         for what, t in (("val", val), ("x", x), ("y", y)):

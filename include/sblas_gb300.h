@@ -174,7 +174,8 @@ SBLAS_API int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_va
  * Inspector: a stable bucket sort of the entries by row gives A's row-ordered
  * structure and the permutation to it (sblas_csc_analyse, into `work`);
  * executor: the values gathered into row order and the CSR tile kernel
- * (sblas_dcscmv_analysed, with the same work, colptr/rowidx unchanged):
+ * (sblas_dcscmv_analysed, with the same work, colptr/rowidx unchanged;
+ * val == NULL: the values last bound with sblas_csc_bind_values):
  * no atomics, bit-reproducible.  sblas_dcscmv runs both.  Rows need not be
  * sorted inside a column.  work: sblas_cscmv_workspace_bytes(m, n, nnz)
  * bytes, 256-byte aligned (sblas_dcscmv: or NULL for a library-owned
@@ -187,6 +188,12 @@ SBLAS_API int sblas_csc_analyse(int m, int n, long long nnz, const int *colptr,
                                 const int *rowidx, void *work, size_t work_bytes, void *stream);
 SBLAS_API int sblas_dcscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
                                     const double *x, double beta, double *y, void *work,
+                                    size_t work_bytes, void *stream);
+/* Keeps `val` (CSC order) in row order inside the analysis in `work`;
+ * sblas_dcscmv_analysed with val == NULL then uses these values and skips
+ * the per-call gather (a CSR product's cost).  Bind again after the values
+ * change. */
+SBLAS_API int sblas_csc_bind_values(int m, int n, long long nnz, const double *val, void *work,
                                     size_t work_bytes, void *stream);
 
 /* Row-sorted COO row indices -> CSR row pointer (int[m + 1]). */

@@ -8,7 +8,7 @@ into row order, then the CSR tile kernel).  Checked here: the golden
 fixtures (the reference's own CPU loop), random matrices with empty and very
 long columns, unsorted rows inside columns, row counts needing two and three
 digit passes, alpha/beta, NaN in y with beta = 0, run-to-run bit equality,
-and the analysed plan reused with new values.  The conversions (CSC -> CSR,
+the analysed plan reused with new values and with values bound once.  The conversions (CSC -> CSR,
 A -> A^T with its permutation) are compared with numpy's stable sort
 exactly.
 """
@@ -102,6 +102,11 @@ def test_cscmv_random_against_oracle(sblas_lib, cuda, m, n, nnz, long_col):
     plan(cv2, xd, y2, 0.5, 0.0)
     ref = O.csc_spmv(m, n, colptr, rowidx, -2.0 * val, x, np.zeros(m), 0.5, 0.0)
     assert _rel(y2.cpu().numpy(), ref) <= TOL
+    # values bound once (kept in row order): calls without values, same bits
+    plan.bind(cv)
+    y3 = torch.zeros(m, dtype=torch.float64, device=cuda)
+    plan(None, xd, y3)
+    assert torch.equal(y1, y3)
 
 
 def test_cscmv_unsorted_rows_and_empty(sblas_lib, cuda):
