@@ -106,11 +106,13 @@ constexpr size_t layout_bytes(int r)
 }
 
 // Rows of a tile held in shared memory: TILE / 4 + 2, unless the CTAs that
-// fit on an SM (at most 4: ~56-70 registers x 224 threads) would then need more
-// than 196 KB of shared memory per SM.  Past that the driver takes the
-// 228-KB carveout, leaves about 28 KB of L1, and random gathers of x run at
-// less than half their rate; the row capacity is then trimmed (by a quarter
-// at most) until the same CTA count fits in 196 KB.
+// fit on an SM (at most 5: 54-62 registers x 224 threads at sigma = 11, fewer
+// for the larger shapes) would then need more than 196 KB of shared memory
+// per SM.  Past that the driver takes the 228-KB carveout, leaves about
+// 28 KB of L1, and random gathers of x run at less than half their rate; the
+// row capacity is then trimmed (by a quarter at most) until the same CTA
+// count fits in 196 KB.  Shapes that still do not fit get a padded request
+// at launch (configure_shape).
 template <int SIGMA, int VK>
 constexpr int rows_in_smem()
 {
@@ -118,7 +120,7 @@ constexpr int rows_in_smem()
     const int r = TC * SIGMA / 4 + 2;
     const size_t cta = layout_bytes<SIGMA, VK>(r) + 1024;   // + the driver's 1 KB per CTA
     int occ = (int)(size_t(228 * 1024) / cta);
-    if (occ > 4) occ = 4;
+    if (occ > 5) occ = 5;
     if ((size_t)occ * cta <= kLimit) return r;
     const size_t budget = kLimit / occ - 1024;
     int t = r;
@@ -882,17 +884,28 @@ __global__ void multi_fixup_kernel(const MultiArgs a, long long tile)
 constexpr int kSigmas[] = {11, 15, 19, 23, 27};
 constexpr int kNumSigmas = sizeof(kSigmas) / sizeof(kSigmas[0]);
 
-// Per device: the kernel's shared-memory attribute, set once, and its
-// resident CTAs per SM (0 = not configured yet); host threads may launch
-// concurrently.  Configuring also loads the kernel onto the device under
-// lazy module loading.
+// Per device: the kernel's shared-memory attribute, set once, its resident
+// CTAs per SM (0 = not configured yet) and the dynamic shared memory each
+// launch requests; host threads may launch concurrently.  Configuring also
+// loads the kernel onto the device under lazy module loading.
+//
+// Random gathers of x run at less than half their rate once the CTAs of an
+// SM hold more than 196 KB of shared memory (the driver then takes the
+// largest carveout and leaves ~28 KB of L1).  rows_in_smem trims each
+// shape's row buffer for four CTAs per SM; a shape whose registers let a
+// fifth CTA in (the smaller layouts: FP32 values and pattern-only at
+// sigma = 11, ~54 registers) would pass the limit again, so the request is
+// padded until the CTAs that fit stay within it (one CTA fewer), down to two
+// CTAs per SM.
 template <int SIGMA, int VK, int AB, class Src = TileArgs>
-int configure_shape(int *out_bps)
+int configure_shape(int *out_bps, size_t *out_smem)
 {
     using L = Layout<SIGMA, VK>;
     auto kfn = tile_spmv_kernel<SIGMA, VK, AB, Src>;
     constexpr int kMaxDev = 64;
+    constexpr size_t kSmemLimit = size_t(195) * 1024;   // per SM, with the 1 KB per CTA
     static std::atomic<int> blocks_per_sm[kMaxDev];
+    static size_t smem_request[kMaxDev];
     static std::mutex config_mu;
     int dev = 0;
     SBLAS_CUDA_TRY(cudaGetDevice(&dev));
@@ -905,32 +918,44 @@ int configure_shape(int *out_bps)
         std::lock_guard<std::mutex> lk(config_mu);
         bps = blocks_per_sm[dev].load(std::memory_order_acquire);
         if (bps == 0) {
-            SBLAS_CUDA_TRY(cudaFuncSetAttribute(
-                kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::TOTAL));
-            SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn, CTA_THREADS,
-                                                                         L::TOTAL));
+            size_t req = L::TOTAL;
+            for (;;) {
+                SBLAS_CUDA_TRY(cudaFuncSetAttribute(
+                    kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req));
+                SBLAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kfn,
+                                                                             CTA_THREADS, req));
+                // (never down to one CTA per SM: measured slower than the
+                // small-L1 carveout with two, banded sigma 27 947 -> 1464 us)
+                if (bps <= 2 || (size_t)bps * (req + 1024) <= kSmemLimit) break;
+                // just enough that one CTA fewer fits in the SM's 228 KB
+                const size_t next = ((size_t(228) * 1024 / bps - 1024 + 128) + 127) & ~size_t(127);
+                if (next <= req || next > size_t(227) * 1024) break;
+                req = next;
+            }
             if (bps < 1) {
                 set_error(SBLAS_ERR_UNSUPPORTED, "tile shape sigma=%d does not fit on this GPU",
                           SIGMA);
                 return SBLAS_ERR_UNSUPPORTED;
             }
+            smem_request[dev] = req;
             blocks_per_sm[dev].store(bps, std::memory_order_release);
         }
     }
     *out_bps = bps;
+    if (out_smem) *out_smem = smem_request[dev];
     return SBLAS_OK;
 }
 
 template <int SIGMA, int VK, int AB, class Src = TileArgs>
 int launch_shape(const Src &a, cudaStream_t stream)
 {
-    using L = Layout<SIGMA, VK>;
     auto kfn = tile_spmv_kernel<SIGMA, VK, AB, Src>;
     int bps = 0;
-    const int rc = configure_shape<SIGMA, VK, AB, Src>(&bps);
+    size_t smem = 0;
+    const int rc = configure_shape<SIGMA, VK, AB, Src>(&bps, &smem);
     if (rc != SBLAS_OK) return rc;
     const int grid = min(a.ntiles, bps * device_num_sms());
-    kfn<<<grid, CTA_THREADS, L::TOTAL, stream>>>(a);
+    kfn<<<grid, CTA_THREADS, smem, stream>>>(a);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }
@@ -1085,9 +1110,9 @@ int tile_preload_f64(int sigma)
     switch (sigma) {
 #define SBLAS_PRELOAD(S)                                                            \
     case S:                                                                         \
-        rc = configure_shape<S, VAL_F64, 0>(&bps);                                  \
-        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 1>(&bps);              \
-        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 2>(&bps);              \
+        rc = configure_shape<S, VAL_F64, 0>(&bps, nullptr);                         \
+        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 1>(&bps, nullptr);     \
+        if (rc == SBLAS_OK) rc = configure_shape<S, VAL_F64, 2>(&bps, nullptr);     \
         break;
         SBLAS_PRELOAD(11)
         SBLAS_PRELOAD(15)
