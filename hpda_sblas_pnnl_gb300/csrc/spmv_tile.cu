@@ -381,6 +381,24 @@ __device__ __forceinline__ double widen_f32(float v)
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 
+// The same widening for a normal FP32 number (exponent field 1..254): sign,
+// exponent rebased by 896 and significand moved in three integer
+// operations.  The compute warps take it for a chunk when no lane's chunk
+// holds a zero, a subnormal, an infinity or a NaN (their exponent field is 0
+// or 255: ((bits >> 23) + 1) & 0xFE == 0), which a warp vote decides; the
+// general widening above costs about twice the instructions, and on the
+// banded matrix the FP32 form was bound by instruction issue.
+__device__ __forceinline__ double widen_normal_f32(unsigned u)
+{
+    const unsigned hi = (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u) | (u & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+__device__ __forceinline__ bool f32_not_normal(unsigned u)
+{
+    return (((u >> 23) + 1u) & 0xFEu) == 0u;
+}
+
 // Compute warp: for each tile of the CTA, one chunk of SIGMA consecutive
 // nonzeros per lane.  Row sums completed inside the chunk go to the carry
 // buffer of the tile's parity; the chunk's head (first segment of a row
@@ -468,24 +486,47 @@ __device__ __forceinline__ void compute_warp(const Src &src, const Smem<SIGMA, V
         int head_row = -1;
         double head_val = 0.0;
         double *headv = sm.headv(p);
+        // FP32 values: whether the whole warp may take the short widening
+        // (every lane votes, also lanes without data; the values are read
+        // again in the chain, which keeps the registers of the 54-register
+        // shape and its five CTAs per SM)
+        bool f32_general = false;
+        if constexpr (VK == VAL_F32) {
+            unsigned odd = 0u;
+            if (cnt > 0 && !warp_slow) {
+#pragma unroll
+                for (int j = 0; j < SIGMA; ++j)
+                    odd |= f32_not_normal(__float_as_uint(vst[c0 + (j < cnt ? j : 0)])) ? 1u : 0u;
+            }
+            f32_general = __any_sync(0xffffffffu, odd != 0u);
+        }
         if (cnt > 0 && !warp_slow) {
             // branch-free FMA chain: at a row start the running sum is stored
             // (the first segment to the thread's head slot when the row began
             // in an earlier chunk) and restarted with a select
-            double *dst = sb ? &headv[t] : &rval[r0 - R0];
-            double *nxt = &rval[r0 + 1 - R0];
+            auto chain = [&](auto value_of) {
+                double *dst = sb ? &headv[t] : &rval[r0 - R0];
+                double *nxt = &rval[r0 + 1 - R0];
 #pragma unroll
-            for (int j = 0; j < SIGMA; ++j) {
-                const bool b = (mask >> j) & 1u;
-                if (b) *dst = sum;
-                dst = b ? nxt : dst;
-                nxt = b ? nxt + 1 : nxt;
-                sum = b ? 0.0 : sum;
-                if (j < cnt) {
-                    if constexpr (VK == VAL_PATTERN) sum += xv[j];
-                    else if constexpr (VK == VAL_F32) sum = fma(widen_f32(vst[c0 + j]), xv[j], sum);
-                    else sum = fma((double)vst[c0 + j], xv[j], sum);
+                for (int j = 0; j < SIGMA; ++j) {
+                    const bool b = (mask >> j) & 1u;
+                    if (b) *dst = sum;
+                    dst = b ? nxt : dst;
+                    nxt = b ? nxt + 1 : nxt;
+                    sum = b ? 0.0 : sum;
+                    if (j < cnt) {
+                        if constexpr (VK == VAL_PATTERN) sum += xv[j];
+                        else sum = fma(value_of(j), xv[j], sum);
+                    }
                 }
+            };
+            if constexpr (VK == VAL_F32) {
+                if (f32_general)
+                    chain([&](int j) { return widen_f32(vst[c0 + j]); });
+                else
+                    chain([&](int j) { return widen_normal_f32(__float_as_uint(vst[c0 + j])); });
+            } else {
+                chain([&](int j) { return (double)vst[c0 + j]; });
             }
             if (sb && mask != 0u) head_row = r0;
         } else if (cnt > 0) {
@@ -727,8 +768,13 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
     }
 }
 
+// CTAs per SM the registers must allow: five for the sigma = 11 shapes
+// whose shared memory fits five (FP32 values, pattern-only), else no bound.
+template <int SIGMA, int VK>
+constexpr int min_ctas() { return (SIGMA == 11 && VK != VAL_F64) ? 5 : 1; }
+
 template <int SIGMA, int VK, int AB, class Src>
-__global__ void __launch_bounds__(CTA_THREADS) tile_spmv_kernel(const Src a)
+__global__ void __launch_bounds__(CTA_THREADS, min_ctas<SIGMA, VK>()) tile_spmv_kernel(const Src a)
 {
     using L = Layout<SIGMA, VK>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
