@@ -61,15 +61,6 @@ class CsrOperator:
         self.bwd = ops.SpmmPlan(self.t_rowptr_c, self.t_col, proto, n=self.m, k=self.k,
                                 s=s_b, row_ids=self.t_rows, m_out=self.n, val_perm=vperm)
 
-    #: run dval on a side stream concurrently with dX in backward
-    concurrent = True
-
-    def side_stream(self) -> torch.cuda.Stream:
-        st = getattr(self, "_side", None)
-        if st is None:
-            st = self._side = torch.cuda.Stream(self.rowptr.device)
-        return st
-
     def _shape(self, rows: int, like: torch.Tensor) -> tuple:
         return (rows,) if like.dim() == 1 else (rows, self.k)
 
@@ -100,27 +91,9 @@ class SpmmFunction(torch.autograd.Function):
         val, x = ctx.saved_tensors
         op = ctx.op
         dval = dx = None
-        want_dx = ctx.needs_input_grad[1]
-        want_dval = ctx.needs_input_grad[0] and val is not None
-        gy = gy.contiguous()
-        if want_dx and want_dval and op.concurrent:
-            # the two adjoint products share only G: dval on a side stream
-            # while dX runs on the current one (dval is bound by the FP64
-            # pipe, dX by its gathers, so they overlap on the SMs)
-            cur = torch.cuda.current_stream(gy.device)
-            side = op.side_stream()
-            dval = torch.empty(op.nnz, dtype=op.value_dtype, device=gy.device)
-            side.wait_stream(cur)
-            with torch.cuda.stream(side):
-                op.fwd.sddmm(gy, x.contiguous(), dval)
-            for t in (gy, x, dval):
-                t.record_stream(side)
+        if ctx.needs_input_grad[1]:
             dx = op.grad_x(val, gy)
-            cur.wait_stream(side)
-            return dval, dx, None
-        if want_dx:
-            dx = op.grad_x(val, gy)
-        if want_dval:
+        if ctx.needs_input_grad[0] and val is not None:
             dval = op.grad_val(gy, x)
         return dval, dx, None
 
