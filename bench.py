@@ -513,6 +513,10 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
         plan_c(cval, x, y)
     csc_ms = statistics.mean(cuda_event_ms(lambda: plan_c(cval, x, y), stream, 10))
     csc_err = float(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+    plan_c.bind(cval)
+    for _ in range(3):
+        plan_c(None, x, y)
+    bound_ms = statistics.mean(cuda_event_ms(lambda: plan_c(None, x, y), stream, 10))
     cw = plan_c.work
     for _ in range(2):
         ops.cscmv(colptr, rowidx, cval, x, y, work=cw)
@@ -524,11 +528,13 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                            "gflops": round(2 * a.nnz / csc_ms / 1e6, 1),
                            "frac": round(bcsc / csc_ms / 1e6 / pk, 4), "us": round(csc_ms * 1e3, 1),
                            "rel_l2_err": csc_err, "inspector_us": round(insp_ms * 1e3, 1),
+                           "bound_values_us": round(bound_ms * 1e3, 1),
                            "one_shot_us": round(once_ms * 1e3, 1),
                            "note": "us/gbs: executor per call (values gathered into row order "
                                    "+ tile kernel); inspector_us: row-ordered structure by the "
-                                   "library's bucket sort, once per pattern; one_shot_us: both "
-                                   "(sblas_dcscmv)"}
+                                   "library's bucket sort, once per pattern; bound_values_us: "
+                                   "executor with values kept in row order (sblas_csc_bind_values); "
+                                   "one_shot_us: inspector + executor (sblas_dcscmv)"}
     del colptr, rowidx, cval
     torch.cuda.empty_cache()
     row = synth.csr_to_coo_rows(a)
