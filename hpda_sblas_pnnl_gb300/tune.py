@@ -91,6 +91,12 @@ def tile_sigma(rowptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor | None
         times[sg] = _time_ms(lambda: plan(x, y), reps)
         del plan
     best = min(times, key=times.get)
+    # shapes within run-to-run noise of each other (a few per cent on one
+    # box) are not told apart by a short timing: keep the library default
+    # unless another shape is clearly faster
+    default = ops.default_sigma(m, col.numel())
+    if default in times and times[default] <= 1.02 * times[best]:
+        best = default
     _CACHE[key] = (best, times)
     return best, times
 

@@ -164,3 +164,41 @@ def test_csc_to_csr_and_transpose_match_stable_sort(sblas_lib, cuda, m, n, nnz):
     np.testing.assert_array_equal(t_c.cpu().numpy(), rowidx)
     back = np.argsort(order, kind="stable")           # CSC position -> CSR position
     np.testing.assert_array_equal(perm.cpu().numpy(), back)
+
+
+@pytest.mark.parametrize("case", ["one_entry", "one_row", "one_column", "every_row_once"])
+def test_sort_edge_cases(sblas_lib, cuda, case):
+    """The bucket sort on degenerate key sets: a single entry, every key
+    equal (all entries in one row: stability alone orders them), one dense
+    column, a permutation matrix (every key once)."""
+    from hpda_sblas_pnnl_gb300 import ops
+    from oracle import oracle as O
+    rng = np.random.default_rng(11)
+    if case == "one_entry":
+        m, n, rows, cols = 5_000_000, 3, np.array([4_999_999]), np.array([1])
+    elif case == "one_row":
+        m, n = 3_000_000, 50_000
+        cols = np.arange(n)
+        rows = np.full(n, 2_999_998)
+    elif case == "one_column":
+        m, n = 70_000, 9
+        rows = np.arange(m)
+        cols = np.full(m, 4)
+    else:
+        m = n = 300_000
+        rows = rng.permutation(m)
+        cols = np.arange(n)
+    vals = rng.standard_normal(rows.size)
+    colptr, rowidx, val = _csc_from_coo(m, n, rows.astype(np.int64), cols.astype(np.int64), vals)
+    x = rng.standard_normal(n)
+    cp, ri, cv, xd = _dev(cuda, colptr, rowidx, val, x)
+    rp, c, v = ops.csc_to_csr(m, n, cp, ri, cv)
+    order = np.argsort(rowidx, kind="stable")
+    ccols = np.repeat(np.arange(n, dtype=np.int32), np.diff(colptr))
+    np.testing.assert_array_equal(c.cpu().numpy(), ccols[order])
+    assert v.cpu().numpy().tobytes() == val[order].tobytes()
+    assert int(rp[-1]) == rows.size and int(rp[0]) == 0
+    y = torch.zeros(m, dtype=torch.float64, device=cuda)
+    ops.cscmv(cp, ri, cv, xd, y)
+    ref = O.csc_spmv(m, n, colptr, rowidx, val, x, np.zeros(m))
+    assert _rel(y.cpu().numpy(), ref) <= TOL
