@@ -501,9 +501,9 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                                "gflops": round(2 * a.nnz / ms / 1e6, 1),
                                "us": round(ms * 1e3, 1), "bytes": b, "rel_l2_err": err,
                                "sigma": sg}
-    # CSC: the inspector (row-ordered structure by the library's bucket sort)
-    # timed apart from the executor (values gathered into row order + tile
-    # kernel); the one-shot call (both) beside them
+    # CSC: the inspector (row-ordered structure by the library's bucket sort,
+    # staging indices) timed apart from the executor (values moved into row
+    # order + tile kernel); the one-shot call (both) beside them
     colptr, rowidx, cval = synth.csr_to_csc(a)
     for _ in range(2):
         plan_c = ops.CscPlan(a.m, colptr, rowidx)
@@ -530,11 +530,13 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                            "rel_l2_err": csc_err, "inspector_us": round(insp_ms * 1e3, 1),
                            "bound_values_us": round(bound_ms * 1e3, 1),
                            "one_shot_us": round(once_ms * 1e3, 1),
-                           "note": "us/gbs: executor per call (values gathered into row order "
-                                   "+ tile kernel); inspector_us: row-ordered structure by the "
-                                   "library's bucket sort, once per pattern; bound_values_us: "
+                           "note": "us/gbs: executor per call (values moved into row order "
+                                   "through 32 MB staging buckets + tile kernel); inspector_us: "
+                                   "row-ordered structure by the library's bucket sort and the "
+                                   "staging indices, once per pattern; bound_values_us: "
                                    "executor with values kept in row order (sblas_csc_bind_values); "
-                                   "one_shot_us: inspector + executor (sblas_dcscmv)"}
+                                   "one_shot_us: sblas_dcscmv (inspector without staging, "
+                                   "values gathered directly, tile kernel)"}
     del colptr, rowidx, cval
     torch.cuda.empty_cache()
     row = synth.csr_to_coo_rows(a)

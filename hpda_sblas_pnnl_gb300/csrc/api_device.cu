@@ -320,7 +320,7 @@ int sblas_csc_analyse(int m, int n, long long nnz, const int *colptr, const int 
         set_error(SBLAS_ERR_ARG, "null device pointer");
         return SBLAS_ERR_ARG;
     }
-    return launch_csc_analyse(m, n, nnz, colptr, rowidx, work, work_bytes,
+    return launch_csc_analyse(m, n, nnz, colptr, rowidx, work, work_bytes, true,
                               static_cast<cudaStream_t>(stream));
 }
 
@@ -332,7 +332,7 @@ int sblas_csc_bind_values(int m, int n, long long nnz, const double *val, void *
         set_error(SBLAS_ERR_ARG, "null device pointer");
         return SBLAS_ERR_ARG;
     }
-    return launch_csc_bind_values(m, n, nnz, val, work, work_bytes,
+    return launch_csc_bind_values(m, n, nnz, val, work, work_bytes, true,
                                   static_cast<cudaStream_t>(stream));
 }
 
@@ -345,7 +345,7 @@ int sblas_dcscmv_analysed(int m, int n, long long nnz, double alpha, const doubl
         set_error(SBLAS_ERR_ARG, "null device pointer");
         return SBLAS_ERR_ARG;
     }
-    return launch_cscmv_analysed(m, n, nnz, alpha, val, x, beta, y, work, work_bytes,
+    return launch_cscmv_analysed(m, n, nnz, alpha, val, x, beta, y, work, work_bytes, true,
                                  static_cast<cudaStream_t>(stream));
 }
 

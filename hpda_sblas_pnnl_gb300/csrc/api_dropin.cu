@@ -339,10 +339,11 @@ spmv_ret run_host(Call c)
             set_error(SBLAS_ERR_ALLOC, "%s: workspace allocation failed", c.name);
             return failed();
         }
-        if (launch_csc_analyse(m, n, nnz, d_ptr, d_idx, w, wb, st) != SBLAS_OK) return failed();
+        if (launch_csc_analyse(m, n, nnz, d_ptr, d_idx, w, wb, false, st) != SBLAS_OK)
+            return failed();
         DROPIN_CUDA(cudaEventRecord(e2, st));   // the inspector counts as format work
-        if (launch_cscmv_analysed(m, n, nnz, c.alpha, d_val, d_x, beta_eff, d_y, w, wb, st) !=
-            SBLAS_OK)
+        if (launch_cscmv_analysed(m, n, nnz, c.alpha, d_val, d_x, beta_eff, d_y, w, wb, false,
+                                  st) != SBLAS_OK)
             return failed();
         if (nnz > 0 && n > 0) tile_work = csc_tile_workspace(w, m, n, nnz);
     } else if (rows > 0) {

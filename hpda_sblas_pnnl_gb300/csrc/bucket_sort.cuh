@@ -217,7 +217,10 @@ struct Payload {
 //     all 32 lanes of a warp for the 32 consecutive entries e0 .. e0 + 31 (in
 //     increasing e0 per warp, so Op::State may carry a cursor);
 //     members key_out, a_out, b_out, d_out: the pass's outputs (a, b, d may
-//     be null: not carried).
+//     be null: not carried);
+//     kPosOut: if true, the member pos_out receives every entry's output
+//     position at its input index (pos_out[e] = position of e); the
+//     payload's b must then be the entry's index e.
 template <class Op>
 __global__ void __launch_bounds__(THREADS, 3) bucket_scatter_kernel(const Op op, long long n,
                                                                  int shift, int nb, int ntiles,
@@ -301,7 +304,8 @@ __global__ void __launch_bounds__(THREADS, 3) bucket_scatter_kernel(const Op op,
     if (tid < nb) toff[tid] = before + v - total;
     __syncthreads();
     // the tile in digit order, with its payloads, in shared memory
-    const bool ha = op.a_out != nullptr, hb = op.b_out != nullptr, hd = op.d_out != nullptr;
+    const bool ha = op.a_out != nullptr, hd = op.d_out != nullptr;
+    const bool hb = op.b_out != nullptr || Op::kPosOut;
 #pragma unroll
     for (int i = 0; i < ITER; ++i) {
         const long long e = wbeg + (long long)i * 32 + lane;
@@ -322,8 +326,9 @@ __global__ void __launch_bounds__(THREADS, 3) bucket_scatter_kernel(const Op op,
         const long long pos = (long long)gbase[d] + (j - toff[d]);
         if (op.key_out) op.key_out[pos] = k;
         if (ha) op.a_out[pos] = st_a[j];
-        if (hb) op.b_out[pos] = st_b[j];
+        if (op.b_out) op.b_out[pos] = st_b[j];
         if (hd) op.d_out[pos] = st_d[j];
+        if constexpr (Op::kPosOut) op.pos_out[st_b[j]] = (int)pos;   // inside the tile's span
     }
 }
 
@@ -435,6 +440,7 @@ struct MoveOp {
     int *a_out;
     int *b_out;
     double *d_out;
+    static constexpr bool kPosOut = false;
     struct State {};
     __device__ int key(long long e) const { return __ldg(key_in + e); }
     __device__ Payload load(State &, long long, int, bool valid, long long e) const
@@ -462,6 +468,7 @@ struct SegmentOp {
     int *a_out;          // segment of the entry, or null
     int *b_out;          // position of the entry, or null
     double *d_out;
+    static constexpr bool kPosOut = false;
     struct State {
         SegCursor c;
     };

@@ -131,17 +131,20 @@ int launch_csc_to_csr(int m, int n, long long nnz, const double *csc_val,
 
 // y = alpha*A*x + beta*y with A in CSC (atomic-free, deterministic):
 // inspector (row-ordered structure + permutation + tile partition into
-// `work`) and executor (value gather + tile kernel).  work:
-// cscmv_workspace_bytes, 256-byte aligned; csc_tile_workspace: the tile
-// workspace inside it (its status word).
+// `work`) and executor (values into row order + tile kernel).  staged: the
+// inspector also builds the staging indices (an analysis reused for many
+// products) and the executor moves values through them; inspector and
+// executor must agree on it.  work: cscmv_workspace_bytes, 256-byte
+// aligned; csc_tile_workspace: the tile workspace inside it (its status
+// word).
 size_t cscmv_workspace_bytes(int m, int n, long long nnz);
 int launch_csc_analyse(int m, int n, long long nnz, const int *colptr, const int *rowidx,
-                       void *work, size_t work_bytes, cudaStream_t stream);
+                       void *work, size_t work_bytes, bool staged, cudaStream_t stream);
 int launch_csc_bind_values(int m, int n, long long nnz, const double *val, void *work,
-                           size_t work_bytes, cudaStream_t stream);
+                           size_t work_bytes, bool staged, cudaStream_t stream);
 int launch_cscmv_analysed(int m, int n, long long nnz, double alpha, const double *val,
                           const double *x, double beta, double *y, void *work,
-                          size_t work_bytes, cudaStream_t stream);
+                          size_t work_bytes, bool staged, cudaStream_t stream);
 int launch_cscmv(int m, int n, long long nnz, double alpha, const double *val,
                  const int *colptr, const int *rowidx, const double *x, double beta, double *y,
                  void *work, size_t work_bytes, cudaStream_t stream);

@@ -185,12 +185,12 @@ def cscmv(colptr: torch.Tensor, rowidx: torch.Tensor, val: torch.Tensor, x: torc
 
 class CscPlan:
     """A CSC pattern (int32 colptr, rowidx) analysed once (sblas_csc_analyse:
-    the row-ordered structure, the permutation to it and the tile
-    partition, held in the plan's workspace); each call runs only the
-    executor (sblas_dcscmv_analysed: the values gathered into row order and
-    the tile kernel), with the values, x and y given per call; bind() keeps
-    one set of values in row order (calls with val=None then skip the
-    gather)."""
+    the row-ordered structure, the permutation to it, the staging indices
+    of patterns above 2^22 entries and the tile partition, held in the
+    plan's workspace); each call runs only the executor
+    (sblas_dcscmv_analysed: the values moved into row order and the tile
+    kernel), with the values, x and y given per call; bind() keeps one set
+    of values in row order (calls with val=None then skip the move)."""
 
     def __init__(self, m: int, colptr: torch.Tensor, rowidx: torch.Tensor):
         dev = _require_cuda(colptr, rowidx)

@@ -8,7 +8,9 @@ into row order, then the CSR tile kernel).  Checked here: the golden
 fixtures (the reference's own CPU loop), random matrices with empty and very
 long columns, unsorted rows inside columns, row counts needing two and three
 digit passes, alpha/beta, NaN in y with beta = 0, run-to-run bit equality,
-the analysed plan reused with new values and with values bound once.  The conversions (CSC -> CSR,
+the analysed plan reused with new values and with values bound once, and
+the plan's staged value move (patterns of several 2^22-entry buckets) bit
+for bit against the one-shot product's direct gather.  The conversions (CSC -> CSR,
 A -> A^T with its permutation) are compared with numpy's stable sort
 exactly.
 """
@@ -164,6 +166,44 @@ def test_csc_to_csr_and_transpose_match_stable_sort(sblas_lib, cuda, m, n, nnz):
     np.testing.assert_array_equal(t_c.cpu().numpy(), rowidx)
     back = np.argsort(order, kind="stable")           # CSC position -> CSR position
     np.testing.assert_array_equal(perm.cpu().numpy(), back)
+
+
+@pytest.mark.parametrize("m,n,nnz,long_col", [
+    (3_000_000, 2_000_000, 9_000_000, None),       # 3 staging buckets of 2^22 entries
+    (6_000_000, 5_000_000, 17_500_000, 123),       # 5 buckets (8 digit values), a long column
+])
+def test_csc_plan_staged_matches_direct_bit_for_bit(sblas_lib, cuda, m, n, nnz, long_col):
+    """An analysed plan above one 2^22-entry bucket moves values through the
+    staging array (a streaming scatter into per-bucket runs, then a gather
+    inside each bucket); the one-shot product gathers them directly.  Both
+    feed the same tile kernel the same row-ordered values: equal bits, and
+    the oracle within 1e-12."""
+    from hpda_sblas_pnnl_gb300 import ops
+    from oracle import oracle as O
+    rng = np.random.default_rng(nnz)
+    colptr, rowidx, val = _random_csc(rng, m, n, nnz, long_col)
+    x = rng.standard_normal(n)
+    y0 = rng.standard_normal(m)
+    cp, ri, cv, xd, y0d = _dev(cuda, colptr, rowidx, val, x, y0)
+    direct = y0d.clone()
+    ops.cscmv(cp, ri, cv, xd, direct, 0.5, -1.25)
+    plan = ops.CscPlan(m, cp, ri)
+    staged = y0d.clone()
+    plan(cv, xd, staged, 0.5, -1.25)
+    assert torch.equal(staged, direct)
+    ref = O.csc_spmv(m, n, colptr, rowidx, val, x, y0, 0.5, -1.25)
+    assert _rel(staged.cpu().numpy(), ref) <= TOL
+    cv2 = torch.flip(cv, [0]).contiguous()               # new values through the plan
+    plan(cv2, xd, staged)
+    direct.zero_()
+    ops.cscmv(cp, ri, cv2, xd, direct)
+    assert torch.equal(staged, direct)
+    plan.bind(cv)                                        # bound values: staged once
+    y3 = y0d.clone()
+    plan(None, xd, y3, 0.5, -1.25)
+    y4 = y0d.clone()
+    ops.cscmv(cp, ri, cv, xd, y4, 0.5, -1.25)
+    assert torch.equal(y3, y4)
 
 
 @pytest.mark.parametrize("case", ["one_entry", "one_row", "one_column", "every_row_once"])
