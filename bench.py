@@ -488,7 +488,7 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
     from hpda_sblas_pnnl_gb300 import ops, synth, tune
     from oracle import oracle as O
     res = {}
-    a, x = synth.powerlaw(seed=args.seed, device=dev)
+    a, x = synth.powerlaw(m=args.m, seed=args.seed, device=dev)
     y = torch.zeros(a.m, dtype=torch.float64, device=dev)
     sg, _ = tune.tile_sigma(a.rowptr, a.col, None, x)
     plan = ops.CsrPlan(a.rowptr, a.col, None, sigma=sg)
@@ -531,7 +531,7 @@ def run_powerlaw_forms_extra(dev, stream, args, timed, threads, pk, forms):
                            "bound_values_us": round(bound_ms * 1e3, 1),
                            "one_shot_us": round(once_ms * 1e3, 1),
                            "note": "us/gbs: executor per call (values moved into row order "
-                                   "through 32 MB staging buckets + tile kernel); inspector_us: "
+                                   "through 8 MB staging buckets + tile kernel); inspector_us: "
                                    "row-ordered structure by the library's bucket sort and the "
                                    "staging indices, once per pattern; bound_values_us: "
                                    "executor with values kept in row order (sblas_csc_bind_values); "

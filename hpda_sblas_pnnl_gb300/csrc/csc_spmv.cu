@@ -214,16 +214,22 @@ __global__ void stage_runs_kernel(long long nnz, int ntiles, int used, int nb,
     }
 }
 
-// out[idx[e]] = e: the inverse of a permutation
+// out[idx[e]] = e: the inverse of a permutation (chunks as above, every
+// index load in flight before the stores)
 __global__ void __launch_bounds__(MOVE_THREADS) invert_kernel(long long nnz,
                                                              const int *__restrict__ idx,
                                                              int *__restrict__ out)
 {
-    for (long long e = (long long)blockIdx.x * MOVE_THREADS + threadIdx.x; e < nnz;
-         e += (long long)gridDim.x * MOVE_THREADS) {
-        const int t = __ldg(idx + e);
-        if (t >= 0 && (long long)t < nnz) out[t] = (int)e;
+    const long long base = (long long)blockIdx.x * MOVE_CHUNK + threadIdx.x;
+    int t[MOVE_ILP];
+#pragma unroll
+    for (int k = 0; k < MOVE_ILP; ++k) {
+        const long long e = base + k * MOVE_THREADS;
+        t[k] = e < nnz ? __ldg(idx + e) : -1;
     }
+#pragma unroll
+    for (int k = 0; k < MOVE_ILP; ++k)
+        if (t[k] >= 0 && (long long)t[k] < nnz) out[t[k]] = (int)(base + k * MOVE_THREADS);
 }
 
 // The staging pass: CSC entries q keyed by their row position inv[q], one
@@ -290,8 +296,7 @@ int launch_csc_analyse(int m, int n, long long nnz, const int *colptr, const int
     int *inv = reinterpret_cast<int *>(w + L.scratch);
     int *slot_row = reinterpret_cast<int *>(w + L.scratch + al256(4 * nn));
     void *pass_work = w + L.scratch + 2 * al256(4 * nn);
-    const long long want = (nnz + MOVE_THREADS - 1) / MOVE_THREADS, cap = 16LL * device_num_sms();
-    const unsigned grid = (unsigned)(want < cap ? want : cap);
+    const unsigned grid = move_grid(nnz);
     invert_kernel<<<grid, MOVE_THREADS, 0, stream>>>(nnz, perm, inv);
     SBLAS_CUDA_TRY(cudaGetLastError());
     StageOp op;
