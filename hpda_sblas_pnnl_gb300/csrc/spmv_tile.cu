@@ -483,48 +483,45 @@ __device__ __forceinline__ void compute_warp(const Src &src, const Smem<SIGMA, V
         }
         const bool warp_slow = __any_sync(0xffffffffu, slow);
         double sum = 0.0;
+        bool f32_odd = false;   // FP32: this lane's chunk holds a value that is not normal
         int head_row = -1;
         double head_val = 0.0;
         double *headv = sm.headv(p);
-        // FP32 values: whether the whole warp may take the short widening
-        // (every lane votes, also lanes without data; the values are read
-        // again in the chain, which keeps the registers of the 54-register
-        // shape and its five CTAs per SM)
-        bool f32_general = false;
-        if constexpr (VK == VAL_F32) {
-            unsigned odd = 0u;
-            if (cnt > 0 && !warp_slow) {
+        // branch-free FMA chain: at a row start the running sum is stored
+        // (the first segment to the thread's head slot when the row began in
+        // an earlier chunk) and restarted with a select
+        auto chain = [&](auto value_of) {
+            sum = 0.0;
+            double *dst = sb ? &headv[t] : &rval[r0 - R0];
+            double *nxt = &rval[r0 + 1 - R0];
 #pragma unroll
-                for (int j = 0; j < SIGMA; ++j)
-                    odd |= f32_not_normal(__float_as_uint(vst[c0 + (j < cnt ? j : 0)])) ? 1u : 0u;
-            }
-            f32_general = __any_sync(0xffffffffu, odd != 0u);
-        }
-        if (cnt > 0 && !warp_slow) {
-            // branch-free FMA chain: at a row start the running sum is stored
-            // (the first segment to the thread's head slot when the row began
-            // in an earlier chunk) and restarted with a select
-            auto chain = [&](auto value_of) {
-                double *dst = sb ? &headv[t] : &rval[r0 - R0];
-                double *nxt = &rval[r0 + 1 - R0];
-#pragma unroll
-                for (int j = 0; j < SIGMA; ++j) {
-                    const bool b = (mask >> j) & 1u;
-                    if (b) *dst = sum;
-                    dst = b ? nxt : dst;
-                    nxt = b ? nxt + 1 : nxt;
-                    sum = b ? 0.0 : sum;
-                    if (j < cnt) {
-                        if constexpr (VK == VAL_PATTERN) sum += xv[j];
-                        else sum = fma(value_of(j), xv[j], sum);
-                    }
+            for (int j = 0; j < SIGMA; ++j) {
+                const bool b = (mask >> j) & 1u;
+                if (b) *dst = sum;
+                dst = b ? nxt : dst;
+                nxt = b ? nxt + 1 : nxt;
+                sum = b ? 0.0 : sum;
+                if (j < cnt) {
+                    if constexpr (VK == VAL_PATTERN) sum += xv[j];
+                    else sum = fma(value_of(j), xv[j], sum);
                 }
-            };
+            }
+        };
+        if (cnt > 0 && !warp_slow) {
             if constexpr (VK == VAL_F32) {
-                if (f32_general)
-                    chain([&](int j) { return widen_f32(vst[c0 + j]); });
-                else
-                    chain([&](int j) { return widen_normal_f32(__float_as_uint(vst[c0 + j])); });
+                // FP32 values read once: the chain widens them the short way
+                // (exact for normal numbers) and notes any zero, subnormal,
+                // infinity or NaN; a warp holding one redoes its chains with
+                // the general widening below, which rewrites the same row
+                // slots (a second read of every value in the common case was
+                // as much shared-memory traffic as FP64 values)
+                unsigned odd = 0u;
+                chain([&](int j) {
+                    const unsigned u = __float_as_uint(vst[c0 + j]);
+                    odd |= f32_not_normal(u) ? 1u : 0u;
+                    return widen_normal_f32(u);
+                });
+                f32_odd = odd != 0u;
             } else {
                 chain([&](int j) { return (double)vst[c0 + j]; });
             }
@@ -563,6 +560,11 @@ __device__ __forceinline__ void compute_warp(const Src &src, const Smem<SIGMA, V
                 }
             }
             headv[t] = head_val;
+        }
+        if constexpr (VK == VAL_F32) {
+            // every lane votes (also lanes without data or on the general path)
+            if (__any_sync(0xffffffffu, f32_odd) && cnt > 0 && !warp_slow)
+                chain([&](int j) { return widen_f32(vst[c0 + j]); });
         }
         // tails stored transposed (thread t at (t % NCW) * 32 + t / NCW) so that
         // the carry pass, where lane l reads threads l*NCW .. l*NCW+NCW-1, is

@@ -206,6 +206,35 @@ def test_csc_plan_staged_matches_direct_bit_for_bit(sblas_lib, cuda, m, n, nnz, 
     assert torch.equal(y3, y4)
 
 
+@pytest.mark.parametrize("m,n,nnz", [
+    (1500, 4000, 1 << 20),            # exactly one bucket: the plan keeps the direct gather
+    (1500, 4000, (1 << 20) + 1),      # a second bucket holding one entry
+    (3, 1_500_000, (1 << 21) + 7),    # three rows, each spanning buckets
+    (700_000, 5, (1 << 21) + 7),      # five columns, each spanning buckets
+])
+def test_csc_plan_staging_bucket_edges(sblas_lib, cuda, m, n, nnz):
+    """Exact entry counts at the 2^20-entry staging bucket boundaries, and
+    rows and columns far longer than a bucket: the plan's staged values
+    equal the one-shot product's direct gather bit for bit."""
+    from hpda_sblas_pnnl_gb300 import ops
+    from oracle import oracle as O
+    rng = np.random.default_rng(nnz + m)
+    key = np.sort(rng.choice(m * n, size=nnz, replace=False))
+    rows, cols = (key % m).astype(np.int64), (key // m).astype(np.int64)
+    colptr, rowidx, val = _csc_from_coo(m, n, rows, cols, rng.standard_normal(nnz))
+    assert rowidx.size == nnz
+    x = rng.standard_normal(n)
+    cp, ri, cv, xd = _dev(cuda, colptr, rowidx, val, x)
+    direct = torch.zeros(m, dtype=torch.float64, device=cuda)
+    ops.cscmv(cp, ri, cv, xd, direct)
+    plan = ops.CscPlan(m, cp, ri)
+    staged = torch.full((m,), float("nan"), dtype=torch.float64, device=cuda)
+    plan(cv, xd, staged)
+    assert torch.equal(staged, direct)
+    ref = O.csc_spmv(m, n, colptr, rowidx, val, x, np.zeros(m))
+    assert _rel(staged.cpu().numpy(), ref) <= TOL
+
+
 @pytest.mark.parametrize("case", ["one_entry", "one_row", "one_column", "every_row_once"])
 def test_sort_edge_cases(sblas_lib, cuda, case):
     """The bucket sort on degenerate key sets: a single entry, every key
