@@ -15,8 +15,8 @@
 //                         (about TILE / nb entries): coalesced stores.
 //                         Every key and payload load of a tile is issued
 //                         before the first is used, and tiles are small
-//                         (~51 KB of shared memory) so that several CTAs per
-//                         SM hide the memory latency.
+//                         (~51 KB of shared memory, 64 registers per thread)
+//                         so that four CTAs per SM hide the memory latency.
 // Entries keep their input order inside every digit (tiles in order, warps in
 // order inside a tile, entries in order inside a warp): a least-significant-
 // digit sequence of passes is a stable sort.  Counts are integers and
@@ -222,7 +222,7 @@ struct Payload {
 //     position at its input index (pos_out[e] = position of e); the
 //     payload's b must then be the entry's index e.
 template <class Op>
-__global__ void __launch_bounds__(THREADS, 3) bucket_scatter_kernel(const Op op, long long n,
+__global__ void __launch_bounds__(THREADS, 4) bucket_scatter_kernel(const Op op, long long n,
                                                                  int shift, int nb, int ntiles,
                                                                  const int *__restrict__ table)
 {
@@ -375,6 +375,10 @@ int scatter_pass(const Op &op, long long n, int shift, int nb, void *work, cudaS
     const size_t smem = scatter_smem_bytes();
     SBLAS_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
+    // four CTAs per SM (~208 KB): the largest shared-memory carveout; this
+    // kernel's loads stream, nothing it reads is reused through L1
+    SBLAS_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        (int)cudaSharedmemCarveoutMaxShared));
     kfn<<<(unsigned)nt, THREADS, smem, stream>>>(op, n, shift, nb, (int)nt, table);
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
