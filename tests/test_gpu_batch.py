@@ -141,7 +141,7 @@ def test_batch_graph_capture_replays_with_new_inputs(sblas_lib, cuda):
 
 @pytest.mark.parametrize("k,split16", [(1, True), (16, True), (16, False)])
 def test_single_matrix_plan_takes_x_y_per_call(sblas_lib, cuda, k, split16):
-    """k = 16 plans run as two k = 8 passes by default (split16)."""
+    """k = 16 plans run as one pass by default, as two k = 8 passes with split16."""
     from hpda_sblas_pnnl_gb300 import ops, synth
     a, _ = synth.powerlaw(m=30_000, mean_deg=20.0, seed=11, device=cuda, values="normal")
     plan = ops.SpmmPlan(a.rowptr, a.col, a.val, n=a.n, k=k, split16=split16)
