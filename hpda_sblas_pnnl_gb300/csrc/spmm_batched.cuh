@@ -284,6 +284,13 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
         const int ldy = a.override_xy ? a.ldy : M->ldy;
         const double alpha = a.override_xy ? a.alpha : M->alpha;
         const double beta = a.override_xy ? a.beta : M->beta;
+        // alpha and beta classified once per unit: a finished element costs
+        // no FP64 operation for alpha = 1, beta = 0 (a compare of doubles
+        // runs on the FP64 pipe too)
+        const int abmode = (beta != 0.0) ? 2 : (alpha != 1.0) ? 1 : 0;
+        auto fin = [&](double v, const double *yp) -> double {
+            return abmode == 0 ? v : abmode == 1 ? alpha * v : fma(alpha, v, beta * *yp);
+        };
         const int m = M->m;
         const int lu = u - M->unit0;
         const int U0 = lu * SH::UNIT;   // row pointers are int32: nnz < 2^31
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
                 } else {
                     double *yr = y + out_row(M, row) * ldy;
 #pragma unroll
-                    for (int c = 0; c < K; ++c) yr[c] = finish(acc[c], alpha, beta, yr + c);
+                    for (int c = 0; c < K; ++c) yr[c] = fin(acc[c], yr + c);
                 }
                 first = false;
 #pragma unroll
@@ -543,7 +550,7 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             } else {
                 double *yr = y + out_row(M, hrow) * ldy;
 #pragma unroll
-                for (int c = 0; c < K; ++c) yr[c] = finish(tot[c], alpha, beta, yr + c);
+                for (int c = 0; c < K; ++c) yr[c] = fin(tot[c], yr + c);
             }
         }
         const int last = cntu > 0 ? (cntu - 1) / S : 0;
@@ -567,14 +574,14 @@ __global__ void __launch_bounds__(CTA) batch_spmm_kernel(const Args a)
             for (int i = lane; i < ne; i += 32) {
                 const int rr = i / K, c = i - rr * K;
                 double *yp = y + out_row(M, E0 + rr) * ldy + c;
-                *yp = finish(rbuf[(E0 - RA + rr) * KP + c], alpha, beta, yp);
+                *yp = fin(rbuf[(E0 - RA + rr) * KP + c], yp);
             }
         } else {
             for (int r = E0 + lane; r < RB; r += 32)
                 if (__ldg(rowptr + r) == __ldg(rowptr + r + 1)) {
                     double *yr = y + out_row(M, r) * ldy;
 #pragma unroll
-                    for (int c = 0; c < K; ++c) yr[c] = finish(0.0, alpha, beta, yr + c);
+                    for (int c = 0; c < K; ++c) yr[c] = fin(0.0, yr + c);
                 }
         }
     }
