@@ -172,10 +172,12 @@ SBLAS_API int sblas_csc_to_csr(int m, int n, long long nnz, const double *csc_va
  * rowidx[nnz], val[nnz]), the device form of spMV_mgpu_baseline_csc
  * (src/dspmv_mgpu_baseline_csc.cu:131-135 runs it as a transposed csrmv).
  * Inspector: a stable bucket sort of the entries by row gives A's row-ordered
- * structure and the permutation to it (sblas_csc_analyse, into `work`);
- * executor: the values gathered into row order and the CSR tile kernel
- * (sblas_dcscmv_analysed, with the same work, colptr/rowidx unchanged;
- * val == NULL: the values last bound with sblas_csc_bind_values):
+ * structure and the permutation to it (sblas_csc_analyse, into `work`;
+ * patterns above 2^20 entries also get staging indices); executor: the
+ * values moved into row order (through L2-resident staging buckets after
+ * sblas_csc_analyse; one direct gather in sblas_dcscmv) and the CSR tile
+ * kernel (sblas_dcscmv_analysed, with the same work, colptr/rowidx
+ * unchanged; val == NULL: the values last bound with sblas_csc_bind_values):
  * no atomics, bit-reproducible.  sblas_dcscmv runs both.  Rows need not be
  * sorted inside a column.  work: sblas_cscmv_workspace_bytes(m, n, nnz)
  * bytes, 256-byte aligned (sblas_dcscmv: or NULL for a library-owned
