@@ -139,13 +139,13 @@ def test_batch_graph_capture_replays_with_new_inputs(sblas_lib, cuda):
             assert rel_l2(y.cpu().numpy(), ref) <= RTOL_L2
 
 
-@pytest.mark.parametrize("k,split16", [(1, True), (16, True), (16, False)])
+@pytest.mark.parametrize("k,split16", [(1, True), (8, False), (16, True), (16, False)])
 def test_single_matrix_plan_takes_x_y_per_call(sblas_lib, cuda, k, split16):
     """k = 16 plans run as one pass by default, as two k = 8 passes with split16."""
     from hpda_sblas_pnnl_gb300 import ops, synth
     a, _ = synth.powerlaw(m=30_000, mean_deg=20.0, seed=11, device=cuda, values="normal")
     plan = ops.SpmmPlan(a.rowptr, a.col, a.val, n=a.n, k=k, split16=split16)
-    for alpha, beta in ((1.0, 0.0), (-2.0, 0.5)):
+    for alpha, beta in ((1.0, 0.0), (3.0, 0.0), (-2.0, 0.5)):
         shape_x = (a.n, k) if k > 1 else (a.n,)
         shape_y = (a.m, k) if k > 1 else (a.m,)
         x = torch.randn(shape_x, dtype=torch.float64, device=cuda)
@@ -155,6 +155,9 @@ def test_single_matrix_plan_takes_x_y_per_call(sblas_lib, cuda, k, split16):
         torch.cuda.synchronize()
         ref = oracle_block(a.rowptr, a.col, a.val, a.n, x, y0, alpha, beta)
         assert rel_l2(y.cpu().numpy(), ref) <= RTOL_L2
+        y2 = y0.clone()                         # the same bits on a second run
+        plan(x, y2, alpha, beta)
+        assert torch.equal(y, y2)
 
 
 def test_batch_rejects_misaligned_x(sblas_lib, cuda):
