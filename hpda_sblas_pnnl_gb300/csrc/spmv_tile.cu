@@ -199,6 +199,8 @@ struct MatView {
     int rp_tma;
     const int *part;       // part[0], part[1]: the rows the tile owns, [R0, R1)
     double *carry;         // the tile's carry slot
+    int abmode;            // runtime alpha/beta (AB = 3): 0 alpha = 1, beta = 0;
+                           // 1 beta = 0; 2 general (classified on the host)
 };
 
 // Source of tiles: one matrix (TileArgs) or many (MultiArgs, below).  Both
@@ -210,7 +212,7 @@ __device__ __forceinline__ MatView view_of(const TileArgs &a, int tile, int)
 {
     return MatView{a.m,      a.nnz,   (long long)tile * TILE, a.val,   a.rowptr,
                    a.col,    a.x,     a.y,                    a.alpha, a.beta,
-                   a.use_tma, a.rp_tma, a.row_part + tile,    a.carry + tile};
+                   a.use_tma, a.rp_tma, a.row_part + tile,    a.carry + tile, 2};
 }
 
 // One matrix of a multi-matrix launch (the batched single-right-hand-side
@@ -230,6 +232,7 @@ struct MultiMat {
     int rp_tma;
     double alpha;
     double beta;
+    int abmode;   // 0: alpha = 1, beta = 0; 1: beta = 0; 2: general
 };
 
 struct MultiArgs {
@@ -261,7 +264,8 @@ __device__ __forceinline__ MatView view_of(const MultiArgs &a, int tile, int mat
     const int lt = tile - M->tile0;
     return MatView{M->m,       M->nnz,    (long long)lt * TILE, M->val,  M->rowptr,
                    M->col,     M->x,      M->y,                 M->alpha, M->beta,
-                   M->use_tma, M->rp_tma, a.part + M->part_off + lt, a.carry + tile};
+                   M->use_tma, M->rp_tma, a.part + M->part_off + lt, a.carry + tile,
+                   M->abmode};
 }
 
 // A bounded wait gave up: the launch's status word and the sticky word.
@@ -276,11 +280,13 @@ __device__ __forceinline__ void report_timeout(const Src &a)
 // only at run time (matrices of a multi-matrix launch each have their own).
 template <int AB>
 __device__ __forceinline__ double finish_row(double v, double alpha, double beta,
-                                             const double *yp)
+                                             const double *yp, int abmode)
 {
     if (AB == 0) return v;                               // alpha = 1, beta = 0
     if (AB == 1) return alpha * v;                       // beta = 0
-    if (AB == 3 && beta == 0.0) return alpha == 1.0 ? v : alpha * v;
+    // AB = 3: the matrix's case, classified on the host (a compare of
+    // doubles per row would run on the FP64 pipe)
+    if (AB == 3 && abmode != 2) return abmode == 0 ? v : alpha * v;
     return fma(alpha, v, beta * __ldg(yp));              // general
 }
 
@@ -543,7 +549,7 @@ __device__ __forceinline__ void compute_warp(const Src &src, const Smem<SIGMA, V
                     } else if (fits) {
                         rval[r - R0] = sum;
                     } else {
-                        a.y[r] = finish_row<AB>(sum, alpha, beta, a.y + r);
+                        a.y[r] = finish_row<AB>(sum, alpha, beta, a.y + r, a.abmode);
                     }
                     first_seg = false;
                     sum = 0.0;
@@ -685,7 +691,7 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
                 } else if (fits) {
                     rval[key - R0] = total;                  // complete row
                 } else {
-                    a.y[key] = finish_row<AB>(total, alpha, beta, a.y + key);
+                    a.y[key] = finish_row<AB>(total, alpha, beta, a.y + key, a.abmode);
                 }
             };
             if (lane == 0) *a.carry = 0.0;
@@ -749,7 +755,7 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
             cin[tt] = 0.0;
             if (hr >= 0) {
                 if (fits) rval[hr - R0] = hv;
-                else a.y[hr] = finish_row<AB>(hv, alpha, beta, a.y + hr);
+                else a.y[hr] = finish_row<AB>(hv, alpha, beta, a.y + hr, a.abmode);
             }
         }
         __syncwarp();
@@ -757,13 +763,13 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
         const int nr = R1 - R0;
         if (fits) {
             for (int r = lane; r < nr; r += 32) {
-                a.y[R0 + r] = finish_row<AB>(rval[r], alpha, beta, a.y + R0 + r);
+                a.y[R0 + r] = finish_row<AB>(rval[r], alpha, beta, a.y + R0 + r, a.abmode);
                 rval[r] = 0.0;
             }
         } else {
             for (int rr = R0 + lane; rr < R1; rr += 32)
                 if (__ldg(a.rowptr + rr) == __ldg(a.rowptr + rr + 1))
-                    a.y[rr] = finish_row<AB>(0.0, alpha, beta, a.y + rr);
+                    a.y[rr] = finish_row<AB>(0.0, alpha, beta, a.y + rr, a.abmode);
         }
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(sm.cempty(p));
@@ -1251,6 +1257,7 @@ void fill_multi_mat(void *dst, const void *val, const int *rowptr, const int *co
     M.rp_tma = (reinterpret_cast<uintptr_t>(rowptr) & 15) == 0 ? 1 : 0;
     M.alpha = alpha;
     M.beta = beta;
+    M.abmode = (beta != 0.0) ? 2 : (alpha != 1.0) ? 1 : 0;
     *static_cast<MultiMat *>(dst) = M;
 }
 
