@@ -198,3 +198,37 @@ def test_row_ids_write_listed_rows_only(sblas_lib, cuda, k):
     assert rel_l2(yy[keep], full[keep]) <= RTOL_L2
     rest = np.setdiff1d(np.arange(m), keep)
     assert (yy[rest] == 7.0).all()
+
+
+@pytest.mark.parametrize("k", [8, 16])
+@pytest.mark.parametrize("s", [4, 8])
+def test_row_lengths_at_group_and_unit_boundaries(sblas_lib, cuda, k, s):
+    """The k >= 8 kernel splits each unit of 32*s nonzeros into 32/k groups
+    of k*s: rows of exactly one group, one more or one less, rows that fill
+    a unit or cross several, empty rows between them and at the ends, in
+    every order.  Within 1e-12 of the oracle; the same bits on a rerun."""
+    from hpda_sblas_pnnl_gb300 import ops
+    h, unit = k * s, 32 * s
+    lengths = [0, 1, h - 1, h, h + 1, 2 * h, unit, unit + 1, 3 * unit + 7, 2, 0, 0]
+    rng = np.random.default_rng(1000 * k + s)
+    deg = np.array([lengths[i] for i in rng.integers(0, len(lengths), 400)] + [0, 0])
+    deg = np.concatenate([[0], deg])
+    m, n = deg.size, 5000
+    rp = np.zeros(m + 1, np.int32)
+    rp[1:] = np.cumsum(deg)
+    col = np.concatenate([np.sort(rng.choice(n, size=d, replace=False)) for d in deg]).astype(np.int32)
+    val = rng.standard_normal(col.size)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    x = torch.rand((n, k), dtype=torch.float64, device=cuda) * 2 - 1
+    y0 = torch.rand((m, k), dtype=torch.float64, device=cuda) * 2 - 1
+    for alpha, beta in ((1.0, 0.0), (0.5, 0.0), (1.5, -0.25)):
+        plan = ops.SpmmPlan(t(rp), t(col), t(val), n=n, k=k, s=s)
+        y = y0.clone()
+        plan(x, y, alpha, beta)
+        y2 = y0.clone()
+        plan(x, y2, alpha, beta)
+        torch.cuda.synchronize()
+        ref = O.csr_spmm(m, n, rp, col, val, x.cpu().numpy(), y0.cpu().numpy(), alpha, beta)
+        assert rel_l2(y.cpu().numpy(), ref) <= RTOL_L2, (alpha, beta)
+        assert torch.equal(y, y2)
+        plan.close()
