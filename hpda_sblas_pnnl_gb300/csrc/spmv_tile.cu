@@ -101,7 +101,7 @@ constexpr size_t layout_bytes(int r)
     const size_t meta = align16(rptr + size_t(STAGES) * rslot * 4);
     const size_t rval = align16(meta + size_t(STAGES) * 16);
     const size_t tailv = align16(rval + 2 * size_t(r) * 8);
-    const size_t cmeta = align16(tailv + 6 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
+    const size_t cmeta = align16(tailv + 4 * size_t(TC) * 8 + 4 * size_t(TC) * 4);
     return align16(cmeta + 2 * 16) + (2 * STAGES + 4) * 8;
 }
 
@@ -145,8 +145,7 @@ struct Layout {
     static constexpr size_t RVAL = align16(META + size_t(STAGES) * 16);
     static constexpr size_t TAILV = align16(RVAL + 2 * size_t(RCAP) * 8);
     static constexpr size_t HEADV = TAILV + 2 * size_t(TC) * 8;
-    static constexpr size_t CIN = HEADV + 2 * size_t(TC) * 8;
-    static constexpr size_t TAILK = CIN + 2 * size_t(TC) * 8;
+    static constexpr size_t TAILK = HEADV + 2 * size_t(TC) * 8;
     static constexpr size_t HEADK = TAILK + 2 * size_t(TC) * 4;
     static constexpr size_t CMETA = align16(HEADK + 2 * size_t(TC) * 4);
     // mbarriers: full[STAGES], empty[STAGES], cfull[2], cempty[2]
@@ -302,7 +301,6 @@ struct Smem {
     __device__ double *rval(int p) const { return reinterpret_cast<double *>(base + L::RVAL) + size_t(p) * L::RCAP; }
     __device__ double *tailv(int p) const { return reinterpret_cast<double *>(base + L::TAILV) + p * TC; }
     __device__ double *headv(int p) const { return reinterpret_cast<double *>(base + L::HEADV) + p * TC; }
-    __device__ double *cin(int p) const { return reinterpret_cast<double *>(base + L::CIN) + p * TC; }
     __device__ int *tailk(int p) const { return reinterpret_cast<int *>(base + L::TAILK) + p * TC; }
     __device__ int *headk(int p) const { return reinterpret_cast<int *>(base + L::HEADK) + p * TC; }
     __device__ int *cmeta(int p) const { return reinterpret_cast<int *>(base + L::CMETA) + 4 * p; }
@@ -649,7 +647,8 @@ __device__ __forceinline__ void producer_warp(const Src &src, const Smem<SIGMA, 
 //   sequentially (NCW tails per lane, work-efficient), a 5-step segmented
 //   shuffle scan joins runs crossing lanes; each run total goes to the head
 //   of the chunk where the row ends, to a complete row, or to the tile carry;
-//   head pass: head + carry-in, one converged add per chunk;
+//   head pass: the heads (with the run each joins, added by the carry pass:
+//   an add only where a run meets a head) out to their rows;
 //   epilogue: alpha/beta once per row, coalesced stores of y.
 template <int SIGMA, int VK, int AB, class Src>
 __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, VK> &sm,
@@ -657,7 +656,6 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
 {
     constexpr int PER = NCW;  // tails reduced per lane
     constexpr int TILE = Layout<SIGMA, VK>::TILE;
-    double *cin = sm.cin(par);
     // this warp takes the tiles of parity `par` (the CTA's tiles i = par,
     // par + 2, ...): the carry buffers are double-buffered by that parity
     for (int i = par, tile = blockIdx.x + par * (int)gridDim.x; tile < src.ntiles;
@@ -678,14 +676,14 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
         const double *tailv = sm.tailv(p);
         const int *tailk = sm.tailk(p);
         const int *headk = sm.headk(p);
-        const double *headv = sm.headv(p);
+        double *headv = sm.headv(p);
 
         // ---------------- carry pass -------------------------------------
         {
             auto emit = [&](int key, double total, int after) {
                 if (key < 0) return;
                 if (after < TC && headk[after] == key) {
-                    cin[after] = total;                      // joins a head
+                    headv[after] += total;                   // joins a head (its one run)
                 } else if (after >= TC && key == R1) {
                     *a.carry = total;                        // continues in next tile
                 } else if (fits) {
@@ -717,7 +715,11 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
                         emit(prevk, acc, ii);
                     }
                 }
-                acc = (brk ? 0.0 : acc) + tailv[q * 32 + lane];
+                // the first tail starts the sum (no add: partial sums are
+                // never -0, so 0 + t == t bit for bit); the FP64 pipe bounds
+                // the banded matrices, and every add here is one of its slots
+                if (q == 0) acc = tailv[lane];
+                else acc = (brk ? 0.0 : acc) + tailv[q * 32 + lane];
                 prevk = key;
             }
             const bool single = !broke;
@@ -726,10 +728,15 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
             const int kl_prev = __shfl_up_sync(0xffffffffu, kl, 1);
             bool f = (lane == 0) || !single || (kl != kl_prev);
             // segmented scan across lanes, only where a lane's last run
-            // continues from its left neighbour somewhere in the warp
-            if (__any_sync(0xffffffffu, !f)) {
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
+            // continues from its left neighbour somewhere in the warp, and
+            // only as many steps as the longest such chain of lanes needs
+            // (the steps after those add 0 to every lane)
+            const unsigned contm = __ballot_sync(0xffffffffu, !f);
+            if (contm != 0u) {
+                const unsigned starts = ~contm & ((2u << lane) - 1u);
+                const int lrun = lane - (31 - __clz(starts));   // lanes joined from the left
+                const int maxrun = (int)__reduce_max_sync(0xffffffffu, (unsigned)lrun);
+                for (int d = 1; d <= maxrun; d <<= 1) {
                     const double So = __shfl_up_sync(0xffffffffu, S, d);
                     const bool fo = __shfl_up_sync(0xffffffffu, f, d);
                     const bool take = (lane >= d) && !f;
@@ -746,13 +753,12 @@ __device__ __forceinline__ void epilogue_warp(const Src &src, const Smem<SIGMA, 
             if (lane == 31 || next_first != kl) emit(kl, S, base + PER);
         }
         __syncwarp();
-        // ---------------- head pass: one converged add per chunk ----------
+        // ---------------- head pass: heads out to their rows ---------------
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int tt = q * 32 + lane;
             const int hr = headk[tt];
-            const double hv = headv[tt] + cin[tt];
-            cin[tt] = 0.0;
+            const double hv = headv[tt];   // the head with the run it joins added
             if (hr >= 0) {
                 if (fits) rval[hr - R0] = hv;
                 else a.y[hr] = finish_row<AB>(hv, alpha, beta, a.y + hr, a.abmode);
@@ -802,7 +808,6 @@ __global__ void __launch_bounds__(CTA_THREADS, min_ctas<SIGMA, VK>()) tile_spmv_
         ptx::fence_mbar_init();
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
-    for (int i = tid; i < 2 * TC; i += CTA_THREADS) sm.cin(0)[i] = 0.0;
     __syncthreads();
     if (warp == NCW)
         producer_warp<SIGMA, VK, Src>(a, sm, lane, ptx::policy_evict_first());
