@@ -132,5 +132,16 @@ __device__ __forceinline__ double2 ldg_x2(const double2 *p, uint64_t policy)
     return v;
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic
+// stream serialisation may start before the previous kernel of its stream
+// has finished; griddep_wait() then blocks until that kernel has completed
+// and its writes are visible (a no-op without such a launch).
+// griddep_launch_dependents() lets the next kernel start early.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace ptx
 }  // namespace sblas

@@ -41,6 +41,8 @@
 #include <climits>
 #include <mutex>
 
+#include <utility>
+
 #include "ptx.cuh"
 #include "sblas_internal.h"
 
@@ -809,6 +811,9 @@ __global__ void __launch_bounds__(CTA_THREADS, min_ctas<SIGMA, VK>()) tile_spmv_
     }
     for (int i = tid; i < 2 * L::RCAP; i += CTA_THREADS) sm.rval(0)[i] = 0.0;
     __syncthreads();
+    // launched right behind the tile partition: the set-up above overlapped
+    // its end; nothing in global memory is read before it has finished
+    ptx::griddep_wait();
     if (warp == NCW)
         producer_warp<SIGMA, VK, Src>(a, sm, lane, ptx::policy_evict_first());
     else if (warp > NCW)
@@ -843,6 +848,7 @@ __global__ void tile_partition_kernel(int m, long long nnz, int ntiles, long lon
                                       const int *__restrict__ rowptr, int *__restrict__ part)
 {
     (void)nnz;
+    ptx::griddep_launch_dependents();   // the tile kernel may start its set-up
     const int stride = gridDim.x * blockDim.x;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g == 0) {
@@ -860,6 +866,7 @@ __global__ void tile_partition_quad_kernel(int m, int ntiles, long long tile,
                                            const int *__restrict__ rowptr,
                                            int *__restrict__ part)
 {
+    ptx::griddep_launch_dependents();   // the tile kernel may start its set-up
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g == 0) {
@@ -895,6 +902,7 @@ __global__ void tile_fixup_kernel(int ntiles, long long tile, double alpha,
                                   const double *__restrict__ carry, double *__restrict__ y,
                                   const int *__restrict__ status)
 {
+    ptx::griddep_wait();   // launched behind the tile kernel: its carries are complete
     const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (k >= ntiles) return;
     if (*status != 0) return;
@@ -1005,6 +1013,26 @@ int configure_shape(int *out_bps, size_t *out_smem)
     return SBLAS_OK;
 }
 
+// A launch with programmatic stream serialisation: the kernel may start
+// while the previous kernel of the stream finishes, and waits for it
+// (ptx::griddep_wait) before it reads global memory.
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kfn)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t stream, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kfn, std::forward<Args>(args)...);
+}
+
 template <int SIGMA, int VK, int AB, class Src = TileArgs>
 int launch_shape(const Src &a, cudaStream_t stream)
 {
@@ -1014,7 +1042,7 @@ int launch_shape(const Src &a, cudaStream_t stream)
     const int rc = configure_shape<SIGMA, VK, AB, Src>(&bps, &smem);
     if (rc != SBLAS_OK) return rc;
     const int grid = min(a.ntiles, bps * device_num_sms());
-    kfn<<<grid, CTA_THREADS, smem, stream>>>(a);
+    SBLAS_CUDA_TRY(launch_pdl(kfn, dim3(grid), dim3(CTA_THREADS), smem, stream, a));
     SBLAS_CUDA_TRY(cudaGetLastError());
     return SBLAS_OK;
 }
@@ -1333,8 +1361,8 @@ int launch_tile_spmv(int m, int n, long long nnz, double alpha, const void *val,
     if (ntiles > 1) {
         const int threads = 256;
         const int blocks = (ntiles - 1 + threads - 1) / threads;
-        tile_fixup_kernel<<<blocks, threads, 0, stream>>>(ntiles, tile, alpha, rowptr, part, carry,
-                                                         y, status);
+        SBLAS_CUDA_TRY(launch_pdl(tile_fixup_kernel, dim3(blocks), dim3(threads), 0, stream,
+                                  ntiles, tile, alpha, rowptr, part, carry, y, status));
         SBLAS_CUDA_TRY(cudaGetLastError());
     }
     return SBLAS_OK;
